@@ -1,0 +1,325 @@
+"""Benchmark: matrix-free XXZ H*v on the L=1000, N_down=4 chain sector (k=0).
+
+Workload (one "step" = one complex(8) H*v over the whole sector, D ~ 4.1e7
+representatives): periodic XXZ chain L=1000, nearest-neighbour Jxy=1, Jz=0.5,
+next-nearest J2xy=J2z=0.3, h=0, sector N_down=4, k=0.  Synthetic: the bond
+list is generated, x is a seeded random vector.
+
+metric  = algorithmic HBM bytes of one H*v / time, with
+          B = D*(16 [x_i] + 16 [y_i] + 8 [list_s_i] + 8 [list_r_i])
+            + nnz_off*(16 [x_id] + 8 [list_r_id])
+          nnz_off = exact number of off-diagonal (row, col) entries.
+value   = B / device time per step (inputs resident in HBM, x and y 663 MB
+          each, larger than L2), CUDA events on the launching stream.
+e2e     = the same B / wall time of qs3g_hv called with HOST buffers
+          (pinned), i.e. H2D of x + kernel + D2H of y every step.
+
+--impl reference times the CPU restatement of ham_to_vec_wave_vector (the
+reference has no GPU path and cannot index this sector with its 32-bit
+integers) on the host cores over a bounded sample of rows, extrapolated to a
+full H*v.  N>1 GPUs run independent replicas (the path needs no exchange on
+one sector; multi-GPU sharding is not built).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_SITES, NOD = 1000, 4
+J1, J2 = (1.0, 0.5), (0.3, 0.3)
+WORKLOAD = "xxz_chain_L1000_Ndown4_k0_J1(1,0.5)_J2(0.3,0.3)_complex128_hv"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_record():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 3 + k and s[3 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    backend = os.environ.get("QS3G_BENCH_BACKEND", "nccl")
+    dist.init_process_group(backend=backend)
+    return dist.get_rank(), dist.get_world_size(), int(os.environ.get("LOCAL_RANK", "0")), dist
+
+
+def max_over_ranks(v: float, dist, device=None) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device.index]) if device.type == "cuda" else dist.barrier()
+        else:
+            dist.barrier()
+
+
+def chain_lists_cpu(nthreads):
+    """Sector lists for the workload, enumerated on the CPU (anchored candidates)."""
+    from oracle import oracle as O
+    return O.chain_sector_lists(L_SITES, NOD, 0, nthreads)
+
+
+def run_reference(args, rank, world, dist):
+    from oracle import oracle as O
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    ls, lr = chain_lists_cpu(nthreads)
+    D = len(ls)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(D) + 1j * rng.standard_normal(D)
+    from ed_gb300 import inputs
+    bonds, jxy, jz = inputs.chain_bonds(L_SITES, J1, J2)
+    m = O.Model(L_SITES, L_SITES, 1, 1, bonds, jxy, jz, kmax=NOD + 2)
+    sec = O.Sector(m, NOD, (0, 0, 0), ls, lr)
+    # calibrate a sample of about args.cpu_seconds / (steps + warmup) per step
+    r0 = D // 3
+    t0 = time.perf_counter()
+    sec.hv(x, rows=(r0, r0 + 2000), nthreads=nthreads)
+    per_row = (time.perf_counter() - t0) / 2000
+    rows = int(max(2000, min(D - r0, args.cpu_seconds / max(1, args.steps + args.warmup) / per_row)))
+    nnz_rows = O.count_offdiag_rows(sec, r0, r0 + rows, nthreads)
+    Bs = rows * 48 + nnz_rows * 24
+    for _ in range(args.warmup):
+        sec.hv(x, rows=(r0, r0 + rows), nthreads=nthreads)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sec.hv(x, rows=(r0, r0 + rows), nthreads=nthreads)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.mean(ts))
+    value = Bs / t / 1e9
+    sample = f"{rows} rows of {D} (rows {r0}..{r0 + rows - 1}), extrapolated per byte to a full H*v"
+    line = {
+        "impl": "reference", "metric": "hv_algorithmic_hbm_gbs", "value": value, "unit": "GB/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sector_dim": D},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank, dist):
+    import torch
+    from ed_gb300 import capi, inputs
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    bonds, jxy, jz = inputs.chain_bonds(L_SITES, J1, J2)
+    h = capi.Handle(L_SITES, L_SITES, 1, 1, bonds, jxy, jz)
+    stream = torch.cuda.current_stream(dev)
+    h.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    D = h.build_sector(NOD, (0, 0, 0))
+    torch.cuda.synchronize(dev)
+    t_build = time.perf_counter() - t0
+    nnz = int(h.connection_table_count())
+    B = D * 48 + nnz * 24
+    g = torch.Generator(device="cpu").manual_seed(1234 + rank)
+    xr = torch.randn(D, 2, dtype=torch.float64, generator=g)
+    x = torch.view_as_complex(xr).to(dev)
+    y = torch.empty_like(x)
+    # warm-up
+    for _ in range(args.warmup):
+        h.hv_device(x.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize(dev)
+    # timed region: inputs (663 MB each) exceed the 129 MB L2, no flush needed
+    n0 = capi.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(dist, dev)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            h.hv_device(x.data_ptr(), y.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier(dist, dev)
+    launches = capi.kernel_launches() - n0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(ms, dist, dev)
+    value = world * B / (ms * 1e-3) / 1e9
+    # e2e: host buffers through the C ABI (H2D x + H*v + D2H y every step)
+    xh = torch.empty(D, dtype=torch.complex128, pin_memory=True)
+    xh.copy_(x.cpu())
+    yh = torch.empty(D, dtype=torch.complex128, pin_memory=True)
+    xnp, ynp = xh.numpy(), yh.numpy()
+    h.hv_host_into(xnp, ynp)
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier(dist, dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.hv_host_into(xnp, ynp)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e = max_over_ranks(t_e2e, dist, dev)
+    # check the e2e result against the device result (same x)
+    yd = y.cpu().numpy()
+    assert np.abs(ynp - yd).max() <= 1e-12 * np.abs(yd).max()
+    peak, peak_kind = peaks()
+    achieved = B / (ms * 1e-3) / 1e9
+    tr = traffic_record().get("hv_chain64", {})
+    line = {
+        "metric": "hv_algorithmic_hbm_gbs", "value": value, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sector_dim": D, "nnz_offdiag": nnz,
+                   "bytes_per_hv": B, "l2": "inputs larger than L2 (x, y 663 MB each), no flush",
+                   "parallelism": f"replicas{world}", "sector_build_s": t_build},
+        "hv_per_s": world * 1e3 / ms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": tr.get("dram_bytes_per_launch"),
+                     "traffic_source": tr.get("source")},
+        "e2e": {"value": world * B / t_e2e / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 16 * D,
+                "d2h_bytes_per_step": 16 * D, "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        ls, lr = h.get_sector()
+        from oracle import oracle as O
+        om = O.Model(L_SITES, L_SITES, 1, 1, bonds, jxy, jz, kmax=NOD + 2)
+        sec = O.Sector(om, NOD, (0, 0, 0), ls, lr)
+        xc = x.cpu().numpy()
+        r0 = D // 3
+        t0 = time.perf_counter()
+        sec.hv(xc, rows=(r0, r0 + 2000), nthreads=nthreads)
+        per_row = (time.perf_counter() - t0) / 2000
+        rows = int(max(2000, min(D - r0, args.cpu_seconds / per_row)))
+        nnz_rows = O.count_offdiag_rows(sec, r0, r0 + rows, nthreads)
+        t0 = time.perf_counter()
+        sec.hv(xc, rows=(r0, r0 + rows), nthreads=nthreads)
+        tc = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": (rows * 48 + nnz_rows * 24) / tc / 1e9, "unit": "GB/s",
+                                "cores": nthreads, "kind": "port",
+                                "sample": f"{rows} rows of {D} timed, extrapolated per byte"}
+    if args.solve and rank == 0:
+        line["gs_solve"] = solve_bench(h, D, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    h.close()
+
+
+def solve_bench(h, D, args):
+    out = {}
+    for name, prec in (("fp64_random", 0), ("fp32store_random", 1)):
+        t0 = time.perf_counter()
+        r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec,
+                    conv_mode=1, seed=7, want_psi=False, allow_unconverged=True)
+        dt = time.perf_counter() - t0
+        out[name] = {"seconds": dt, "hv": r["iters"], "E0": float(r["ene"][0]),
+                     "resid": float(r["resid"][0]), "converged": bool(r["converged"])}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--solve", action="store_true")
+    ap.add_argument("--nok", type=int, default=4)
+    ap.add_argument("--nom", type=int, default=24)
+    ap.add_argument("--maxrestart", type=int, default=2000)
+    ap.add_argument("--tol", type=float, default=5e-11)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local_rank, dist = dist_setup()
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world, dist)
+        else:
+            run_gpu(args, rank, world, local_rank, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

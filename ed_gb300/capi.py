@@ -1,0 +1,256 @@
+"""ctypes binding of libqs3g.so (include/qs3g.h).
+
+This is the host-side view of the C ABI used by the tests and bench.py.  It
+mirrors the QS3 module procedures it replaces: ``Handle.hv`` is
+ham_to_vec_wave_vector (ham2vec_v3.f90:37-72), ``Handle.trlan`` is
+lancz_eigen_val_complex (eigen_solver.f90:69-261), ``Handle.dsf`` is
+calcu_Sq_a + calcu_DSF_wavevector (get_expectation_values.f90:281-605) and
+``cfrac`` is DSFLan (source_DSFLan/main.f90).  Every call checks the status
+code and raises :class:`QS3GError` with the library's message.
+
+There is no CPU fallback: if the CUDA library cannot be loaded, the import of
+this module's functions raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqs3g.so")
+
+OK, EINVAL, ENOMEM, ENOTCONV, EITERCAP, ECUDA, ESTATE, ERANGE, ENOTSUP, EBREAKDOWN = range(10)
+HOST, DEVICE = 0, 1
+
+EXPORTS = [
+    "qs3g_create", "qs3g_destroy", "qs3g_build_sector", "qs3g_get_sector", "qs3g_hv", "qs3g_hv32",
+    "qs3g_connection_table", "qs3g_connection_table_rows", "qs3g_trlan", "qs3g_lanczos", "qs3g_dsf",
+    "qs3g_cfrac", "qs3g_last_error", "qs3g_kernel_launches", "qs3g_set_stream", "qs3g_sync",
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+class QS3GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"qs3g error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load the shared library (building it first if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            from . import build as _b
+            _b.build()
+        L = C.CDLL(p)
+        vp, ip, dp, i64p = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int64)
+        L.qs3g_last_error.restype = C.c_char_p
+        L.qs3g_last_error.argtypes = [vp]
+        L.qs3g_kernel_launches.restype = C.c_int64
+        for name in EXPORTS:
+            if name not in ("qs3g_last_error", "qs3g_kernel_launches"):
+                getattr(L, name).restype = C.c_int
+        L.qs3g_destroy.argtypes = [vp]
+        _lib = L
+        return L
+
+
+def _i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v):
+    return C.byref(C.c_double(float(v)))
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _check(rc, h=None):
+    if rc != OK:
+        msg = load().qs3g_last_error(h).decode(errors="replace")
+        raise QS3GError(rc, msg)
+
+
+def kernel_launches() -> int:
+    return int(load().qs3g_kernel_launches())
+
+
+class Handle:
+    """One qs3g handle: lattice, bonds and the current sector."""
+
+    def __init__(self, NOS, LX, LY, LZ, bonds, Jxy, Jz):
+        L = load()
+        bonds = np.ascontiguousarray(np.asarray(bonds, dtype=np.int32).reshape(-1, 2))
+        self.NOS, self.LX, self.LY, self.LZ = int(NOS), int(LX), int(LY), int(LZ)
+        self.NOxxz = bonds.shape[0]
+        sJ = np.ascontiguousarray(np.concatenate([np.asarray(Jxy, np.float64) * 0.5,
+                                                  np.asarray(Jz, np.float64) * 0.25]))
+        h = C.c_void_p()
+        rc = L.qs3g_create(C.byref(h), _i(self.NOS), _i(self.LX), _i(self.LY), _i(self.LZ),
+                           _i(self.NOxxz), _ptr(bonds.reshape(-1)), _ptr(sJ))
+        _check(rc, None)
+        self.h = h
+        self.D = None
+        self.nod = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().qs3g_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr: int):
+        """Queue the handle's work on a caller-owned cudaStream_t (e.g. torch's)."""
+        _check(load().qs3g_set_stream(self.h, C.c_void_p(stream_ptr)), self.h)
+
+    def sync(self):
+        _check(load().qs3g_sync(self.h), self.h)
+
+    def build_sector(self, nod, K=(0, 0, 0)):
+        D = C.c_int64()
+        _check(load().qs3g_build_sector(self.h, _i(nod), _i(K[0]), _i(K[1]), _i(K[2]), C.byref(D)), self.h)
+        self.D = int(D.value)
+        self.nod = int(nod)
+        return self.D
+
+    def get_sector(self):
+        ls = np.zeros(self.D, np.int64)
+        lr = np.zeros(self.D, np.float64)
+        _check(load().qs3g_get_sector(self.h, _ptr(ls), _ptr(lr)), self.h)
+        return ls, lr
+
+    def hv(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        assert x.shape == (self.D,)
+        y = np.zeros(self.D, np.complex128)
+        _check(load().qs3g_hv(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
+        return y
+
+    def hv_host_into(self, x, y):
+        """y = H x through the host-pointer form (x, y: complex128 arrays, e.g. pinned)."""
+        assert x.dtype == np.complex128 and y.dtype == np.complex128
+        assert x.flags.c_contiguous and y.flags.c_contiguous
+        _check(load().qs3g_hv(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
+
+    def connection_table_count(self):
+        nnz = C.c_int64(0)
+        _check(load().qs3g_connection_table(self.h, None, None, None, None, C.byref(nnz)), self.h)
+        return int(nnz.value)
+
+    def hv_device(self, x_ptr: int, y_ptr: int):
+        """y = H x for device pointers (complex128), on the handle's stream."""
+        _check(load().qs3g_hv(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)
+
+    def hv32(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex64)
+        y = np.zeros(self.D, np.complex64)
+        _check(load().qs3g_hv32(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
+        return y
+
+    def hv32_device(self, x_ptr: int, y_ptr: int):
+        _check(load().qs3g_hv32(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)
+
+    def connection_table(self, rows=None):
+        L = load()
+        nnz = C.c_int64(0)
+        if rows is None:
+            _check(L.qs3g_connection_table(self.h, None, None, None, None, C.byref(nnz)), self.h)
+        else:
+            r0, r1 = C.c_int64(rows[0] + 1), C.c_int64(rows[1])
+            _check(L.qs3g_connection_table_rows(self.h, C.byref(r0), C.byref(r1), None, None, None,
+                                                None, C.byref(nnz)), self.h)
+        n = int(nnz.value)
+        row = np.zeros(n, np.int64)
+        col = np.zeros(n, np.int64)
+        ell = np.zeros((n, 3), np.int32)
+        bond = np.zeros(n, np.int32)
+        if n:
+            if rows is None:
+                _check(L.qs3g_connection_table(self.h, _ptr(row), _ptr(col), _ptr(ell), _ptr(bond),
+                                               C.byref(nnz)), self.h)
+            else:
+                _check(L.qs3g_connection_table_rows(self.h, C.byref(r0), C.byref(r1), _ptr(row),
+                                                    _ptr(col), _ptr(ell), _ptr(bond), C.byref(nnz)),
+                       self.h)
+        return row, col, ell, bond
+
+    def trlan(self, NOE, NOK, NOM, maxitr=10000, tol=1e-12, precision=0, conv_mode=0, seed=1,
+              start=None, want_psi=True, allow_unconverged=False):
+        ene = np.zeros(NOE)
+        psi = np.zeros((NOE, self.D), np.complex128) if want_psi else None
+        resid = np.zeros(NOE)
+        iters = C.c_int(0)
+        st = None if start is None else np.ascontiguousarray(start, np.complex128)
+        sd = C.c_uint64(int(seed))
+        rc = load().qs3g_trlan(self.h, _i(NOE), _i(NOK), _i(NOM), _i(maxitr), _d(tol), _i(precision),
+                               _i(conv_mode), _i(0 if st is None else 1), C.byref(sd), _ptr(st),
+                               _ptr(ene), _ptr(psi), C.byref(iters), _ptr(resid))
+        if rc == ENOTCONV and allow_unconverged:
+            pass
+        else:
+            _check(rc, self.h)
+        return dict(ene=ene, psi=psi, iters=int(iters.value), resid=resid, converged=(rc == OK))
+
+    def lanczos(self, maxitr=10000, minitr=20, itrint=5, tol=1e-14, seed=1, start=None):
+        ene = np.zeros(1)
+        psi = np.zeros(self.D, np.complex128)
+        iters = C.c_int(0)
+        st = None if start is None else np.ascontiguousarray(start, np.complex128)
+        sd = C.c_uint64(int(seed))
+        _check(load().qs3g_lanczos(self.h, _i(maxitr), _i(minitr), _i(itrint), _d(tol),
+                                   _i(0 if st is None else 1), C.byref(sd), _ptr(st), _ptr(ene),
+                                   _ptr(psi), C.byref(iters)), self.h)
+        return dict(ene=float(ene[0]), psi=psi, iters=int(iters.value))
+
+    def dsf(self, psi, ene1, spsmsz, qvecs, Spos, itr_dsf, rfield=0.0):
+        qv = np.ascontiguousarray(np.asarray(qvecs, np.float64).reshape(-1, 3))
+        nq = qv.shape[0]
+        sp = np.ascontiguousarray(np.asarray(Spos, np.float64).reshape(-1))
+        alpha = np.zeros((nq, itr_dsf))
+        beta2 = np.zeros((nq, itr_dsf))
+        norm1 = np.zeros(nq)
+        E0 = np.zeros(nq)
+        nlev = np.zeros(nq, np.int32)
+        psi = np.ascontiguousarray(psi, np.complex128)
+        _check(load().qs3g_dsf(self.h, _ptr(psi), _d(ene1), _i(spsmsz), _i(nq), _ptr(qv.reshape(-1)),
+                               _ptr(sp), _i(itr_dsf), _d(rfield), _ptr(alpha), _ptr(beta2),
+                               _ptr(norm1), _ptr(E0), _ptr(nlev)), self.h)
+        return dict(alpha=alpha, beta2=beta2, norm1=norm1, E0=E0, nlev=nlev)
+
+
+def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
+    """DSFLan continued fraction for nq spectra: alpha/beta2 are (nq, ldab)."""
+    alpha = np.ascontiguousarray(np.atleast_2d(alpha), np.float64)
+    beta2 = np.ascontiguousarray(np.atleast_2d(beta2), np.float64)
+    nq, ld = alpha.shape
+    nlev = np.ascontiguousarray(np.atleast_1d(nlev), np.int32)
+    norm1 = np.ascontiguousarray(np.atleast_1d(norm1), np.float64)
+    E0 = np.ascontiguousarray(np.atleast_1d(E0), np.float64)
+    omega = np.ascontiguousarray(omega, np.float64)
+    S = np.zeros((nq, len(omega)))
+    _check(load().qs3g_cfrac(_i(nq), _i(ld), _ptr(nlev), _ptr(alpha), _ptr(beta2), _ptr(norm1),
+                             _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega), _i(1 if compat else 0),
+                             _ptr(S)))
+    return S

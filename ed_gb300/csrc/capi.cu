@@ -1,0 +1,333 @@
+// capi.cu -- the extern "C" boundary of libqs3g.so (declared in include/qs3g.h).
+//
+// Every entry point catches qs3g::Error and CUDA failures and turns them into
+// a status code plus a message retrievable with qs3g_last_error; nothing
+// throws across the boundary.  Scalars arrive by pointer (Fortran bind(C)
+// by-reference convention).
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "krylov.h"
+#include "qs3g_internal.cuh"
+
+using namespace qs3g;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_last_error;
+
+void set_error(qs3g_ctx* h, const std::string& msg) {
+  if (h) h->last_error = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error = msg;
+}
+
+template <class F>
+int guarded(qs3g_ctx* h, F&& f) {
+  try {
+    return f();
+  } catch (const Error& e) {
+    set_error(h, e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_error(h, "host allocation failed");
+    return QS3G_ENOMEM;
+  } catch (const std::exception& e) {
+    set_error(h, e.what());
+    return QS3G_EINVAL;
+  }
+}
+
+// Site adjacency, per-site Jz sums and device copies of the bond data.
+void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int* p_xxz, const double* sJint,
+                 cudaStream_t st) {
+  QS3G_REQUIRE(NOS >= 1 && LX >= 1 && LY >= 1 && LZ >= 1, QS3G_EINVAL, "lattice sizes must be >= 1");
+  QS3G_REQUIRE((int64_t)LX * LY * LZ == NOS, QS3G_EINVAL, "NOS must equal LX*LY*LZ");
+  QS3G_REQUIRE(NOS < 65535, QS3G_ERANGE, "NOS must be < 65535");
+  QS3G_REQUIRE(NOxxz >= 0 && NOxxz < 65535, QS3G_ERANGE, "NOxxz must be < 65535");
+  m.NOS = NOS; m.LX = LX; m.LY = LY; m.LZ = LZ; m.NOxxz = NOxxz;
+  m.chain = (LY == 1 && LZ == 1);
+  m.bits = bits_for(NOS);
+  m.p1.resize(NOxxz); m.p2.resize(NOxxz); m.sJxy.resize(NOxxz); m.sJz.resize(NOxxz);
+  m.Sz_all = 0.0;
+  m.Sz_site.assign(NOS + 1, 0.0);
+  std::vector<std::vector<uint32_t>> adj(NOS + 1);
+  for (int b = 0; b < NOxxz; ++b) {
+    int a = p_xxz[2 * b], c = p_xxz[2 * b + 1];
+    QS3G_REQUIRE(a >= 1 && a <= NOS && c >= 1 && c <= NOS, QS3G_EINVAL, "bond site out of range");
+    if (a > c) std::swap(a, c);  // input_param.f90:97-101
+    m.p1[b] = a; m.p2[b] = c;
+    m.sJxy[b] = sJint[b];
+    m.sJz[b] = sJint[NOxxz + b];
+    m.Sz_all += m.sJz[b];
+    if (a != c) {
+      adj[a].push_back(((uint32_t)b << 16) | (uint32_t)c);
+      adj[c].push_back(((uint32_t)b << 16) | (uint32_t)a);
+      m.Sz_site[a] += m.sJz[b];
+      m.Sz_site[c] += m.sJz[b];
+    }
+  }
+  m.adj_off.assign(NOS + 2, 0);
+  m.adj.clear();
+  for (int s = 1; s <= NOS; ++s) {
+    m.adj_off[s] = (int)m.adj.size();
+    for (uint32_t w : adj[s]) m.adj.push_back(w);
+  }
+  m.adj_off[NOS + 1] = (int)m.adj.size();
+  m.adj_off[0] = 0;
+  std::vector<int16_t> xyz(4 * (size_t)(NOS + 1), 0);
+  for (int s = 1; s <= NOS; ++s) {
+    const int s0 = s - 1;
+    xyz[4 * s] = (int16_t)(s0 % LX);
+    xyz[4 * s + 1] = (int16_t)((s0 / LX) % LY);
+    xyz[4 * s + 2] = (int16_t)(s0 / (LX * LY));
+  }
+  auto up = [&](auto& dev, const auto& host) {
+    using T = typename std::decay_t<decltype(host)>::value_type;
+    dev.alloc(std::max<size_t>(1, host.size()));
+    if (!host.empty())
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(dev.get(), host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  };
+  up(m.d_adj_off, m.adj_off);
+  up(m.d_adj, m.adj);
+  up(m.d_sJxy, m.sJxy);
+  up(m.d_sJz, m.sJz);
+  up(m.d_Sz_site, m.Sz_site);
+  up(m.d_site_xyz, xyz);
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+const Sector& need_sector(qs3g_ctx* h) {
+  QS3G_REQUIRE(h && h->sector, QS3G_ESTATE, "no sector: call qs3g_build_sector first");
+  return *h->sector;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qs3g_create(qs3g_handle* out, const int* NOS, const int* LX, const int* LY, const int* LZ, const int* NOxxz,
+                const int* p_xxz, const double* sJint) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(out && NOS && LX && LY && LZ && NOxxz, QS3G_EINVAL, "null argument");
+    QS3G_REQUIRE(*NOxxz == 0 || (p_xxz && sJint), QS3G_EINVAL, "null bond arrays");
+    *out = nullptr;
+    std::unique_ptr<qs3g_ctx> h(new qs3g_ctx());
+    QS3G_CHECK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    try {
+      setup_model(h->model, *NOS, *LX, *LY, *LZ, *NOxxz, p_xxz, sJint, h->stream);
+    } catch (...) {
+      cudaStreamDestroy(h->stream);
+      throw;
+    }
+    *out = h.release();
+    return QS3G_OK;
+  });
+}
+
+int qs3g_destroy(qs3g_handle h) {
+  if (!h) return QS3G_OK;
+  cudaStream_t st = h->stream;
+  const bool own = h->own_stream;
+  if (st) cudaStreamSynchronize(st);
+  delete h;
+  if (st && own) cudaStreamDestroy(st);
+  return QS3G_OK;
+}
+
+int qs3g_build_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, int64_t* D_out) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h && NOD && KX && KY && KZ, QS3G_EINVAL, "null argument");
+    const int K[3] = {*KX, *KY, *KZ};
+    std::unique_ptr<Sector> s(new Sector());
+    build_sector(h->model, *NOD, K, *s, h->stream);
+    h->sector = std::move(s);
+    if (D_out) *D_out = h->sector->D;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_get_sector(qs3g_handle h, int64_t* list_s, double* list_r) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    if (s.D == 0) return QS3G_OK;
+    if (list_s)
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(list_s, s.d_list_s.get(), s.D * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (list_r)
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(list_r, s.d_list_r.get(), s.D * 8, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
+// Device staging for the host-pointer forms of H*v: kept in the handle and
+// grown on demand, so repeated calls do not allocate.
+static void* staging(qs3g_ctx* h, int which, size_t bytes) {
+  auto& b = h->stage[which];
+  if (b.n < bytes) b.alloc(bytes);
+  return b.get();
+}
+
+int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(v0 && v1 && where, QS3G_EINVAL, "null argument");
+    if (*where == QS3G_DEVICE) {  // asynchronous on the handle's stream
+      hv64(h->model, s, reinterpret_cast<const double2*>(v1), reinterpret_cast<double2*>(v0), h->stream);
+      return QS3G_OK;
+    }
+    QS3G_REQUIRE(*where == QS3G_HOST, QS3G_EINVAL, "where must be QS3G_HOST or QS3G_DEVICE");
+    const size_t bytes = (size_t)s.D * sizeof(double2);
+    auto* x = static_cast<double2*>(staging(h, 0, bytes));
+    auto* y = static_cast<double2*>(staging(h, 1, bytes));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(x, v1, bytes, cudaMemcpyHostToDevice, h->stream));
+    hv64(h->model, s, x, y, h->stream);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v0, y, bytes, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
+int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* where) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(v0 && v1 && where, QS3G_EINVAL, "null argument");
+    if (*where == QS3G_DEVICE) {  // asynchronous on the handle's stream
+      hv32(h->model, s, reinterpret_cast<const float2*>(v1), reinterpret_cast<float2*>(v0), h->stream);
+      return QS3G_OK;
+    }
+    QS3G_REQUIRE(*where == QS3G_HOST, QS3G_EINVAL, "where must be QS3G_HOST or QS3G_DEVICE");
+    const size_t bytes = (size_t)s.D * sizeof(float2);
+    auto* x = static_cast<float2*>(staging(h, 0, bytes));
+    auto* y = static_cast<float2*>(staging(h, 1, bytes));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(x, v1, bytes, cudaMemcpyHostToDevice, h->stream));
+    hv32(h->model, s, x, y, h->stream);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v0, y, bytes, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
+int qs3g_set_stream(qs3g_handle h, void* stream) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h, QS3G_EINVAL, "null handle");
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->own_stream) {
+      QS3G_CHECK_CUDA(cudaStreamDestroy(h->stream));
+      h->own_stream = false;
+    }
+    h->stream = static_cast<cudaStream_t>(stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_sync(qs3g_handle h) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h, QS3G_EINVAL, "null handle");
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
+int qs3g_connection_table(qs3g_handle h, int64_t* row, int64_t* col, int* ell, int* bond, int64_t* nnz) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(nnz, QS3G_EINVAL, "null nnz");
+    const int64_t cap = *nnz;
+    const int64_t n = connection_table(h->model, s, row, col, ell, bond, row ? cap : 0, h->stream);
+    *nnz = n;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const int64_t* row_last, int64_t* row,
+                               int64_t* col, int* ell, int* bond, int64_t* nnz) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(nnz && row_first && row_last, QS3G_EINVAL, "null argument");
+    const int64_t cap = *nnz;
+    const int64_t n = connection_table_rows(h->model, s, *row_first - 1, *row_last, row, col, ell, bond,
+                                            row ? cap : 0, h->stream);
+    *nnz = n;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, const int* maxitr, const double* tol,
+               const int* precision, const int* conv_mode, const int* start_mode, const uint64_t* seed,
+               const qs3g_cplx* start, double* ene, qs3g_cplx* psi, int* iters, double* resid) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(NOE && NOK && NOM && maxitr && tol && ene, QS3G_EINVAL, "null argument");
+    TrlanParams p;
+    p.NOE = *NOE; p.NOK = *NOK; p.NOM = *NOM; p.maxitr = *maxitr; p.tol = *tol;
+    p.precision = precision ? *precision : 0;
+    p.conv_mode = conv_mode ? *conv_mode : 0;
+    p.seed = seed ? *seed : 1;
+    QS3G_REQUIRE(p.precision == 0 || p.precision == 1, QS3G_EINVAL, "precision must be 0 or 1");
+    QS3G_REQUIRE(p.conv_mode >= 0 && p.conv_mode <= 2, QS3G_EINVAL, "conv_mode must be 0, 1 or 2");
+    const int sm = start_mode ? *start_mode : 0;
+    QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");
+    return trlan(h->model, s, p, sm == 1 ? reinterpret_cast<const double2*>(start) : nullptr, ene,
+                 reinterpret_cast<double2*>(psi), iters, resid, h->stream);
+  });
+}
+
+int qs3g_lanczos(qs3g_handle h, const int* maxitr, const int* minitr, const int* itrint, const double* tol,
+                 const int* start_mode, const uint64_t* seed, const qs3g_cplx* start, double* ene, qs3g_cplx* psi,
+                 int* iters) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(maxitr && minitr && itrint && tol && ene, QS3G_EINVAL, "null argument");
+    const int sm = start_mode ? *start_mode : 0;
+    QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");
+    return lanczos(h->model, s, *maxitr, *minitr, *itrint, *tol,
+                   sm == 1 ? reinterpret_cast<const double2*>(start) : nullptr, seed ? *seed : 1, ene,
+                   reinterpret_cast<double2*>(psi), iters, h->stream);
+  });
+}
+
+int qs3g_dsf(qs3g_handle h, const qs3g_cplx* psi, const double* ene1, const int* spsmsz, const int* nq,
+             const double* qvec, const double* Spos, const int* itr_dsf, const double* rfield, double* alpha,
+             double* beta2, double* norm1, double* E0, int* nlev) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(psi && ene1 && spsmsz && nq && qvec && Spos && itr_dsf && rfield && alpha && beta2 && norm1 &&
+                     E0 && nlev,
+                 QS3G_EINVAL, "null argument");
+    return dsf(h->model, s, reinterpret_cast<const double2*>(psi), *ene1, *spsmsz, *nq, qvec, Spos, *itr_dsf,
+               *rfield, alpha, beta2, norm1, E0, nlev, h->stream);
+  });
+}
+
+int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* alpha, const double* beta2,
+               const double* norm1, const double* E0, const double* eta, const int* nomega, const double* omega,
+               const int* compat, double* S) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(nq && ldab && nlev && alpha && beta2 && norm1 && E0 && eta && nomega && omega && compat && S,
+                 QS3G_EINVAL, "null argument");
+    QS3G_REQUIRE(*nq >= 1 && *ldab >= 1 && *nomega >= 1, QS3G_EINVAL, "sizes must be >= 1");
+    cudaStream_t st;
+    QS3G_CHECK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    try {
+      cfrac(*nq, *ldab, nlev, alpha, beta2, norm1, E0, *eta, *nomega, omega, *compat, S, st);
+    } catch (...) {
+      cudaStreamDestroy(st);
+      throw;
+    }
+    cudaStreamDestroy(st);
+    return QS3G_OK;
+  });
+}
+
+const char* qs3g_last_error(qs3g_handle h) {
+  if (h) return h->last_error.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_last_error.c_str();
+}
+
+int64_t qs3g_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"

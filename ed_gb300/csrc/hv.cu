@@ -1,0 +1,511 @@
+// hv.cu -- matrix-free XXZ H*v over the (NOD, K) representative basis.
+//
+// Replaces ham_to_vec_wave_vector (ham2vec_v3.f90:37-72).  Gather form: each
+// output row is computed by exactly one thread (chains) or one warp (general
+// lattices) and written once, with no atomics, so results are deterministic.
+//
+// Per row the reference loops over all NOxxz bonds; here the loop runs over
+// the bonds incident to the row's NOD down spins (site adjacency, both bond
+// ends listed), which visits every antiparallel bond exactly once:
+//   diagonal  = sum_b sJz_b * (+1 parallel / -1 antiparallel)
+//             = Sz_all - 2 * (sum_{d down} Sz_site[d] - sum_{both-down encounters} sJz_b)
+//   hop       = sJxy_b * list_r(id) / list_r(i) * explist(ell) * v1(id)
+// For chains the representative of each hop comes from chain_rep (O(NOD^2)
+// cyclic-gap keys, same ell rule as representative_SQ); general lattices scan
+// all translations with the 32 lanes of a warp and reduce with shuffles.
+// The row index comes from the sector directory (one 32-byte load) instead of
+// findstate's binary search.
+#include "qs3g_device.cuh"
+#include "qs3g_internal.cuh"
+#include "krylov.h"
+
+namespace qs3g {
+namespace {
+
+template <class F>
+void dispatch_nod(int NOD, F&& f) {
+  switch (NOD) {
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    case 3: f(std::integral_constant<int, 3>{}); break;
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 5: f(std::integral_constant<int, 5>{}); break;
+    case 6: f(std::integral_constant<int, 6>{}); break;
+    case 7: f(std::integral_constant<int, 7>{}); break;
+    case 8: f(std::integral_constant<int, 8>{}); break;
+    default: throw Error(QS3G_ENOTSUP, "NOD > 8 is not instantiated");
+  }
+}
+
+struct HvArgs {
+  int64_t D;
+  int L, NOS, bits, LX, LY, LZ, NT;
+  const uint64_t* conf;
+  const double* list_r;
+  const float* list_r32;
+  const uint32_t* dir;
+  const uint32_t* binomA;
+  const uint64_t* binom;
+  const int* adj_off;
+  const uint32_t* adj;
+  const double* sJxy;
+  const double* sJz;
+  const double* Sz_site;
+  double Sz_all;
+  const double2* chainph;
+  const float2* chainph32;
+  const double2* explist;
+  const int16_t* xyz;
+};
+
+constexpr int kHvThreads = 256;
+
+// ------------------------------------------------------------ chain, complex(8)
+template <int NOD, bool KZERO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain64(HvArgs a, const double2* __restrict__ x,
+                                                           double2* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const double2 xi = x[i];
+  const double ri = __ldg(a.list_r + i);
+  const long long rib = __double_as_longlong(ri);
+  double sdown = 0.0, both = 0.0;
+  double2 accs = make_double2(0.0, 0.0), accd = make_double2(0.0, 0.0);
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    sdown += __ldg(a.Sz_site + d);
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) { both += __ldg(a.sJz + b); continue; }
+      int o[NOD], p[NOD], ell;
+      move_spin<NOD>(n, m, e, o);
+      chain_rep<NOD>(o, a.L, a.bits, p, ell);
+      const int64_t id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
+      if (id < 0) continue;
+      double2 xv = x[id];
+      const double rv = __ldg(a.list_r + id);
+      const double cj = __ldg(a.sJxy + b);
+      if (!KZERO) xv = cmul(__ldg(a.chainph + ell), xv);
+      if (__double_as_longlong(rv) == rib) {
+        accs.x = fma(cj, xv.x, accs.x);
+        accs.y = fma(cj, xv.y, accs.y);
+      } else {
+        const double cw = cj * rv;
+        accd.x = fma(cw, xv.x, accd.x);
+        accd.y = fma(cw, xv.y, accd.y);
+      }
+    }
+  }
+  const double diag = fma(-2.0, sdown - both, a.Sz_all);
+  double2 out = make_double2(fma(diag, xi.x, accs.x), fma(diag, xi.y, accs.y));
+  if (accd.x != 0.0 || accd.y != 0.0) {
+    const double inv = 1.0 / ri;
+    out.x = fma(inv, accd.x, out.x);
+    out.y = fma(inv, accd.y, out.y);
+  }
+  y[i] = out;
+}
+
+// ------------------------------------------------------------ chain, complex(4)
+template <int NOD, bool KZERO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain32(HvArgs a, const float2* __restrict__ x,
+                                                           float2* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const float2 xi = x[i];
+  const float ri = __ldg(a.list_r32 + i);
+  float sdown = 0.f, both = 0.f;
+  float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    sdown += (float)__ldg(a.Sz_site + d);
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) { both += (float)__ldg(a.sJz + b); continue; }
+      int o[NOD], p[NOD], ell;
+      move_spin<NOD>(n, m, e, o);
+      chain_rep<NOD>(o, a.L, a.bits, p, ell);
+      const int64_t id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
+      if (id < 0) continue;
+      float2 xv = x[id];
+      const float cw = (float)__ldg(a.sJxy + b) * __ldg(a.list_r32 + id);
+      if (!KZERO) xv = cmulf(__ldg(a.chainph32 + ell), xv);
+      acc.x = fmaf(cw, xv.x, acc.x);
+      acc.y = fmaf(cw, xv.y, acc.y);
+    }
+  }
+  const float diag = fmaf(-2.f, sdown - both, (float)a.Sz_all);
+  const float inv = 1.0f / ri;
+  y[i] = make_float2(fmaf(diag, xi.x, inv * acc.x), fmaf(diag, xi.y, inv * acc.y));
+}
+
+// ------------------------------------------------------------ general lattice helpers
+template <int NOD>
+__device__ __forceinline__ uint64_t translate_pack(const int (&n)[NOD], int ti, int tj, int tk,
+                                                   const HvArgs& a) {
+  int t[NOD];
+#pragma unroll
+  for (int e = 0; e < NOD; ++e) {
+    const short4 c = reinterpret_cast<const short4*>(a.xyz)[n[e]];
+    int xx = c.x + ti; xx -= (xx >= a.LX) ? a.LX : 0;
+    int yy = c.y + tj; yy -= (yy >= a.LY) ? a.LY : 0;
+    int zz = c.z + tk; zz -= (zz >= a.LZ) ? a.LZ : 0;
+    t[e] = 1 + xx + a.LX * (yy + a.LY * zz);
+  }
+#pragma unroll
+  for (int i = 1; i < NOD; ++i) {
+#pragma unroll
+    for (int j = i; j > 0; --j) {
+      const int lo = min(t[j - 1], t[j]), hi = max(t[j - 1], t[j]);
+      t[j - 1] = lo; t[j] = hi;
+    }
+  }
+  return pack<NOD>(t, a.bits);
+}
+
+__device__ __forceinline__ void tau_to_ijk(int tau, const HvArgs& a, int& i, int& j, int& k) {
+  i = tau % a.LX + 1;
+  const int r = tau / a.LX;
+  j = r % a.LY + 1;
+  k = r / a.LY + 1;
+}
+
+// representative_SQ for a general lattice by one thread (used by the connection table).
+template <int NOD>
+__device__ __forceinline__ uint64_t general_rep_serial(const int (&o)[NOD], const HvArgs& a, int& tau_best) {
+  uint64_t best = ~0ull;
+  tau_best = 0x7fffffff;
+  int tau = 0;
+  for (int k = 1; k <= a.LZ; ++k)
+    for (int j = 1; j <= a.LY; ++j)
+      for (int i = 1; i <= a.LX; ++i, ++tau) {
+        const uint64_t w = translate_pack<NOD>(o, i % a.LX, j % a.LY, k % a.LZ, a);
+        if (w < best) { best = w; tau_best = tau; }
+      }
+  return best;
+}
+
+// ------------------------------------------------------------ general lattice, complex(8), warp per row
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_general64(HvArgs a, const double2* __restrict__ x,
+                                                             double2* __restrict__ y) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const double2 xi = x[i];
+  const double ri = __ldg(a.list_r + i);
+  double sdown = 0.0, both = 0.0;
+  double2 acc = make_double2(0.0, 0.0);
+  const size_t ex1 = (size_t)a.LX + 1, ex2 = ex1 * ((size_t)a.LY + 1);
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    sdown += __ldg(a.Sz_site + d);
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) { both += __ldg(a.sJz + b); continue; }
+      int o[NOD];
+      move_spin<NOD>(n, m, e, o);
+      uint64_t best = ~0ull;
+      int bt = 0x7fffffff;
+      for (int tau = lane; tau < a.NT; tau += 32) {
+        int ti, tj, tk;
+        tau_to_ijk(tau, a, ti, tj, tk);
+        const uint64_t v = translate_pack<NOD>(o, ti % a.LX, tj % a.LY, tk % a.LZ, a);
+        if (v < best) { best = v; bt = tau; }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
+        if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+      }
+      int rep[NOD];
+      unpack<NOD>(best, a.bits, rep);
+      const int64_t id = dir_lookup(a.dir, full_index<NOD>(rep, a.binom, a.NOS));
+      if (id < 0) continue;
+      size_t eidx = 0;
+      if (best != pack<NOD>(o, a.bits)) {
+        int ti, tj, tk;
+        tau_to_ijk(bt, a, ti, tj, tk);
+        eidx = (size_t)ti + ex1 * (size_t)tj + ex2 * (size_t)tk;
+      }
+      const double c = __ldg(a.sJxy + b) * __ldg(a.list_r + id) / ri;
+      const double2 ex = __ldg(a.explist + eidx);
+      const double2 ce = make_double2(c * ex.x, c * ex.y);
+      const double2 tv = cmul(ce, x[id]);
+      acc.x += tv.x;
+      acc.y += tv.y;
+    }
+  }
+  if (lane == 0) {
+    const double diag = fma(-2.0, sdown - both, a.Sz_all);
+    y[i] = make_double2(fma(diag, xi.x, acc.x), fma(diag, xi.y, acc.y));
+  }
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const float2* __restrict__ x,
+                                                             float2* __restrict__ y) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const float2 xi = x[i];
+  const float ri = __ldg(a.list_r32 + i);
+  float sdown = 0.f, both = 0.f;
+  float2 acc = make_float2(0.f, 0.f);
+  const size_t ex1 = (size_t)a.LX + 1, ex2 = ex1 * ((size_t)a.LY + 1);
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    sdown += (float)__ldg(a.Sz_site + d);
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) { both += (float)__ldg(a.sJz + b); continue; }
+      int o[NOD];
+      move_spin<NOD>(n, m, e, o);
+      uint64_t best = ~0ull;
+      int bt = 0x7fffffff;
+      for (int tau = lane; tau < a.NT; tau += 32) {
+        int ti, tj, tk;
+        tau_to_ijk(tau, a, ti, tj, tk);
+        const uint64_t v = translate_pack<NOD>(o, ti % a.LX, tj % a.LY, tk % a.LZ, a);
+        if (v < best) { best = v; bt = tau; }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
+        if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+      }
+      int rep[NOD];
+      unpack<NOD>(best, a.bits, rep);
+      const int64_t id = dir_lookup(a.dir, full_index<NOD>(rep, a.binom, a.NOS));
+      if (id < 0) continue;
+      size_t eidx = 0;
+      if (best != pack<NOD>(o, a.bits)) {
+        int ti, tj, tk;
+        tau_to_ijk(bt, a, ti, tj, tk);
+        eidx = (size_t)ti + ex1 * (size_t)tj + ex2 * (size_t)tk;
+      }
+      const float c = (float)__ldg(a.sJxy + b) * __ldg(a.list_r32 + id) / ri;
+      const double2 ex = __ldg(a.explist + eidx);
+      const float2 tv = cmulf(make_float2(c * (float)ex.x, c * (float)ex.y), x[id]);
+      acc.x += tv.x;
+      acc.y += tv.y;
+    }
+  }
+  if (lane == 0) {
+    const float diag = fmaf(-2.f, sdown - both, (float)a.Sz_all);
+    y[i] = make_float2(fmaf(diag, xi.x, acc.x), fmaf(diag, xi.y, acc.y));
+  }
+}
+
+// ------------------------------------------------------------ connection table
+constexpr int kMaxRowEntries = 64;
+
+template <int NOD>
+__global__ void __launch_bounds__(128) k_conn(HvArgs a, bool chain, int64_t row0, int64_t row1,
+                                              int64_t* counts, const int64_t* offs, int64_t* orow,
+                                              int64_t* ocol, int* oell, int* obond, int* overflow) {
+  const int64_t i = row0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= row1) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  int eb[kMaxRowEntries], ee[kMaxRowEntries];
+  int64_t ec[kMaxRowEntries];
+  int cnt = 0;
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    const int e0 = a.adj_off[d], e1 = a.adj_off[d + 1];
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = a.adj[t];
+      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
+      bool edown = false;
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) continue;
+      int o[NOD];
+      move_spin<NOD>(n, m, e, o);
+      int64_t id;
+      int ellcode;  // chain: translation i; general: tau+1 (0 = identity / minimal)
+      if (chain) {
+        int p[NOD], ell;
+        chain_rep<NOD>(o, a.L, a.bits, p, ell);
+        id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
+        ellcode = ell;
+      } else {
+        int bt;
+        const uint64_t best = general_rep_serial<NOD>(o, a, bt);
+        int rep[NOD];
+        unpack<NOD>(best, a.bits, rep);
+        id = dir_lookup(a.dir, full_index<NOD>(rep, a.binom, a.NOS));
+        ellcode = (best == pack<NOD>(o, a.bits)) ? 0 : bt + 1;
+      }
+      if (id < 0) continue;
+      if (cnt < kMaxRowEntries) { eb[cnt] = b; ee[cnt] = ellcode; ec[cnt] = id; }
+      ++cnt;
+    }
+  }
+  if (cnt > kMaxRowEntries) { atomicExch(overflow, 1); cnt = kMaxRowEntries; }
+  if (counts) { counts[i - row0] = cnt; return; }
+  // order by bond number (ham2vec_v3.f90:56 loops bonds in list order)
+  for (int u = 1; u < cnt; ++u) {
+    const int b = eb[u], e = ee[u];
+    const int64_t c = ec[u];
+    int v = u - 1;
+    while (v >= 0 && eb[v] > b) { eb[v + 1] = eb[v]; ee[v + 1] = ee[v]; ec[v + 1] = ec[v]; --v; }
+    eb[v + 1] = b; ee[v + 1] = e; ec[v + 1] = c;
+  }
+  int64_t w = offs[i - row0];
+  for (int u = 0; u < cnt; ++u, ++w) {
+    orow[w] = i + 1;
+    ocol[w] = ec[u] + 1;
+    obond[w] = eb[u] + 1;
+    int ti = 0, tj = 0, tk = 0;
+    if (chain) {
+      if (ee[u] != 0) { ti = ee[u]; tj = 1; tk = 1; }
+    } else if (ee[u] != 0) {
+      tau_to_ijk(ee[u] - 1, a, ti, tj, tk);
+    }
+    oell[3 * w] = ti; oell[3 * w + 1] = tj; oell[3 * w + 2] = tk;
+  }
+}
+
+HvArgs make_args(const Model& m, const Sector& s) {
+  HvArgs a{};
+  a.D = s.D; a.L = m.NOS; a.NOS = m.NOS; a.bits = m.bits;
+  a.LX = m.LX; a.LY = m.LY; a.LZ = m.LZ; a.NT = m.LX * m.LY * m.LZ;
+  a.conf = s.d_conf.get(); a.list_r = s.d_list_r.get(); a.list_r32 = s.d_list_r32.get();
+  a.dir = s.d_dir.get(); a.binomA = s.d_binomA.get(); a.binom = s.d_binom.get();
+  a.adj_off = m.d_adj_off.get(); a.adj = m.d_adj.get();
+  a.sJxy = m.d_sJxy.get(); a.sJz = m.d_sJz.get(); a.Sz_site = m.d_Sz_site.get(); a.Sz_all = m.Sz_all;
+  a.chainph = s.d_chainph.get(); a.chainph32 = s.d_chainph32.get(); a.explist = s.d_explist.get();
+  a.xyz = m.d_site_xyz.get();
+  return a;
+}
+
+}  // namespace
+
+void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
+  if (s.D == 0) return;
+  const HvArgs a = make_args(m, s);
+  if (s.anchored) {
+    const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+    dispatch_nod(s.NOD, [&](auto c) {
+      if (s.kzero) k_hv_chain64<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      else k_hv_chain64<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
+    });
+    check_launch("k_hv_chain64");
+  } else {
+    hv64_general(m, s, x, y, st);
+  }
+}
+
+void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
+  if (s.D == 0) return;
+  const HvArgs a = make_args(m, s);
+  const unsigned grid = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_hv_general64<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y);
+  });
+  check_launch("k_hv_general64");
+}
+
+void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st) {
+  if (s.D == 0) return;
+  const HvArgs a = make_args(m, s);
+  if (s.anchored) {
+    const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+    dispatch_nod(s.NOD, [&](auto c) {
+      if (s.kzero) k_hv_chain32<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      else k_hv_chain32<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
+    });
+    check_launch("k_hv_chain32");
+  } else {
+    const unsigned grid = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
+    dispatch_nod(s.NOD, [&](auto c) {
+      k_hv_general32<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y);
+    });
+    check_launch("k_hv_general32");
+  }
+}
+
+int64_t connection_table_rows(const Model& m, const Sector& s, int64_t row0, int64_t row1, int64_t* row,
+                              int64_t* col, int* ell, int* bond, int64_t cap, cudaStream_t st) {
+  QS3G_REQUIRE(row0 >= 0 && row1 <= s.D && row0 <= row1, QS3G_EINVAL, "bad row range");
+  const int64_t nr = row1 - row0;
+  if (nr == 0) return 0;
+  const HvArgs a = make_args(m, s);
+  DevBuf<int64_t> d_cnt(nr);
+  DevBuf<int> d_ovf(1);
+  QS3G_CHECK_CUDA(cudaMemsetAsync(d_ovf.get(), 0, sizeof(int), st));
+  const unsigned grid = (unsigned)((nr + 127) / 128);
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, s.anchored, row0, row1, d_cnt.get(), nullptr,
+                                                    nullptr, nullptr, nullptr, nullptr, d_ovf.get());
+  });
+  check_launch("k_conn(count)");
+  std::vector<int64_t> h(nr);
+  int ovf = 0;
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(h.data(), d_cnt.get(), nr * 8, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(&ovf, d_ovf.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  QS3G_REQUIRE(!ovf, QS3G_ERANGE, "a row has more than 64 hops");
+  int64_t nnz = 0;
+  for (int64_t r = 0; r < nr; ++r) { const int64_t t = h[r]; h[r] = nnz; nnz += t; }
+  if (!row) return nnz;
+  QS3G_REQUIRE(nnz <= cap, QS3G_ERANGE, "connection table capacity too small");
+  if (nnz == 0) return 0;
+  DevBuf<int64_t> d_off(nr), d_row(nnz), d_col(nnz);
+  DevBuf<int> d_ell(3 * nnz), d_bond(nnz);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_off.get(), h.data(), nr * 8, cudaMemcpyHostToDevice, st));
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, s.anchored, row0, row1, nullptr, d_off.get(),
+                                                    d_row.get(), d_col.get(), d_ell.get(), d_bond.get(),
+                                                    d_ovf.get());
+  });
+  check_launch("k_conn(emit)");
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(row, d_row.get(), nnz * 8, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(col, d_col.get(), nnz * 8, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(ell, d_ell.get(), 3 * nnz * 4, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(bond, d_bond.get(), nnz * 4, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  return nnz;
+}
+
+int64_t connection_table(const Model& m, const Sector& s, int64_t* row, int64_t* col, int* ell, int* bond,
+                         int64_t cap, cudaStream_t st) {
+  return connection_table_rows(m, s, 0, s.D, row, col, ell, bond, cap, st);
+}
+
+}  // namespace qs3g

@@ -1,0 +1,753 @@
+// krylov.cu -- level-1 kernels, thick-restart Lanczos, plain Lanczos, the
+// dynamical-structure-factor recursion and the continued fraction.
+//
+// Replaces my_l1_blas.f90:5-25 (my_zaxpy, my_zdscal), the BLAS calls zdotc /
+// dznrm2 / zcopy / zscal / zgemm of eigen_solver.f90:69-261 and
+// lanczos.f90:50-152, calcu_Sq_a + calcu_DSF_wavevector
+// (get_expectation_values.f90:281-605) and DSFLan (source_DSFLan/main.f90).
+//
+// Reductions are deterministic: a fixed grid of kRedBlocks blocks each reduce
+// a fixed grid-stride slice in a fixed tree order into a partial, and one
+// block reduces the partials in a fixed order.  All Lanczos scalars (alpha,
+// beta, overlaps) stay in device memory, so a Lanczos cycle is a chain of
+// kernel launches with no host round trip; the host reads the scalars once
+// per restart to solve the NOM x NOM Ritz problem.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "hosteig.h"
+#include "qs3g_device.cuh"
+#include "qs3g_internal.cuh"
+#include "krylov.h"
+
+namespace qs3g {
+
+// ================================================================ reductions
+namespace {
+constexpr int kRedThreads = 256;
+
+template <class T>
+struct Ld;
+template <>
+struct Ld<double2> {
+  static __device__ __forceinline__ double re(const double2& v) { return v.x; }
+  static __device__ __forceinline__ double im(const double2& v) { return v.y; }
+};
+template <>
+struct Ld<float2> {
+  static __device__ __forceinline__ double re(const float2& v) { return (double)v.x; }
+  static __device__ __forceinline__ double im(const float2& v) { return (double)v.y; }
+};
+
+__device__ __forceinline__ double2 block_sum2(double2 v, double2* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
+      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  return sh[0];
+}
+
+// part[b] = sum over the block's slice of conj(x_i) y_i
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_dot_part(const T* __restrict__ x, const T* __restrict__ y,
+                                                          int64_t n, double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T a = x[i], b = y[i];
+    const double ar = Ld<T>::re(a), ai = Ld<T>::im(a), br = Ld<T>::re(b), bi = Ld<T>::im(b);
+    acc.x = fma(ar, br, fma(ai, bi, acc.x));
+    acc.y = fma(ar, bi, fma(-ai, br, acc.y));
+  }
+  const double2 s = block_sum2(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// part[b] = sum |x_i|^2
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_nrm_part(const T* __restrict__ x, int64_t n, double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T a = x[i];
+    const double ar = Ld<T>::re(a), ai = Ld<T>::im(a);
+    acc.x = fma(ar, ar, fma(ai, ai, acc.x));
+  }
+  const double2 s = block_sum2(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// out = sum of np partials (mode 0: complex; 1: sqrt(real) into .x; 2: real)
+__global__ void __launch_bounds__(kRedThreads) k_red_final(const double2* part, int np, double2* out, int mode) {
+  __shared__ double2 sh[kRedThreads];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    acc.x += part[i].x;
+    acc.y += part[i].y;
+  }
+  const double2 s = block_sum2(acc, sh);
+  if (threadIdx.x == 0) {
+    if (mode == 1) *out = make_double2(sqrt(s.x), 0.0);
+    else if (mode == 2) *out = make_double2(s.x, 0.0);
+    else *out = s;
+  }
+}
+
+// ---------------------------------------------------------------- level-1 updates
+// x *= 1/s.x  (my_zdscal with a = 1/beta, eigen_solver.f90:101)
+template <class T>
+__global__ void k_scale_inv(T* x, int64_t n, const double2* s) {
+  const double inv = 1.0 / s->x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T v = x[i];
+    v.x = (decltype(v.x))((double)v.x * inv);
+    v.y = (decltype(v.y))((double)v.y * inv);
+    x[i] = v;
+  }
+}
+
+// w = q - a*v - b*u   (a complex or its real part, b real; u may be null)
+template <class T>
+__global__ void k_lanczos_w(T* w, const T* q, const T* __restrict__ v, const T* __restrict__ u, int64_t n, const double2* a, const double2* b,
+                            int real_alpha) {
+  const double ar = a->x, ai = real_alpha ? 0.0 : a->y;
+  const double br = u ? b->x : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T qv = q[i], vv = v[i];
+    double re = (double)qv.x - (ar * (double)vv.x - ai * (double)vv.y);
+    double im = (double)qv.y - (ar * (double)vv.y + ai * (double)vv.x);
+    if (u) {
+      const T uv = u[i];
+      re -= br * (double)uv.x;
+      im -= br * (double)uv.y;
+    }
+    T o;
+    o.x = (decltype(o.x))re;
+    o.y = (decltype(o.y))im;
+    w[i] = o;
+  }
+}
+
+// y += a*x  (my_zaxpy, my_l1_blas.f90:5-14) with a from device memory, a_sign applied
+template <class T>
+__global__ void k_axpy(T* __restrict__ y, const T* __restrict__ x, int64_t n, const double2* a, double sgn) {
+  const double ar = sgn * a->x, ai = sgn * a->y;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T xv = x[i];
+    T yv = y[i];
+    yv.x = (decltype(yv.x))((double)yv.x + (ar * (double)xv.x - ai * (double)xv.y));
+    yv.y = (decltype(yv.y))((double)yv.y + (ar * (double)xv.y + ai * (double)xv.x));
+    y[i] = yv;
+  }
+}
+
+// ---------------------------------------------------------------- block GEMV for reorthogonalisation
+// part[c*nb + b] = sum over slice of conj(V[:,c]) w   for c < ncols (chunks of 8 columns)
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_gemv_h_part(const T* __restrict__ V, int64_t ldv, int ncols,
+                                                             const T* __restrict__ w, int64_t n, double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  for (int c0 = 0; c0 < ncols; c0 += 8) {
+    double2 acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = make_double2(0.0, 0.0);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      const T b = w[i];
+      const double br = Ld<T>::re(b), bi = Ld<T>::im(b);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (c0 + k < ncols) {
+          const T a = V[(int64_t)(c0 + k) * ldv + i];
+          const double ar = Ld<T>::re(a), ai = Ld<T>::im(a);
+          acc[k].x = fma(ar, br, fma(ai, bi, acc[k].x));
+          acc[k].y = fma(ar, bi, fma(-ai, br, acc[k].y));
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (c0 + k < ncols) {
+        const double2 s = block_sum2(acc[k], sh);
+        if (threadIdx.x == 0) part[(size_t)(c0 + k) * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// out[c] = sgn * sum_b part[c*nb + b]
+__global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part, int nb, int ncols, double2* out) {
+  __shared__ double2 sh[kRedThreads];
+  for (int c = 0; c < ncols; ++c) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      acc.x += part[(size_t)c * nb + i].x;
+      acc.y += part[(size_t)c * nb + i].y;
+    }
+    const double2 s = block_sum2(acc, sh);
+    if (threadIdx.x == 0) out[c] = s;
+    __syncthreads();
+  }
+}
+
+// w -= V[:, :ncols] * coef   (coef from device memory)
+template <class T>
+__global__ void k_gemv_sub(const T* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
+                           T* __restrict__ w, int64_t n) {
+  __shared__ double2 c[128];
+  for (int k = threadIdx.x; k < ncols; k += blockDim.x) c[k] = coef[k];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T wv = w[i];
+    double re = (double)wv.x, im = (double)wv.y;
+    for (int k = 0; k < ncols; ++k) {
+      const T a = V[(int64_t)k * ldv + i];
+      re -= c[k].x * (double)a.x - c[k].y * (double)a.y;
+      im -= c[k].x * (double)a.y + c[k].y * (double)a.x;
+    }
+    T o;
+    o.x = (decltype(o.x))re;
+    o.y = (decltype(o.y))im;
+    w[i] = o;
+  }
+}
+
+// In-place restart V[:, :nok] = V[:, :nom] * C (zgemm + zcopy, eigen_solver.f90:147-149).
+// 32 rows per block; the rows' nom inputs are staged in shared memory first.
+template <class T>
+__global__ void __launch_bounds__(256) k_restart(T* V, int64_t ldv, int nom, int nok, const double2* __restrict__ C,
+                                                 int64_t n) {
+  extern __shared__ double2 sm[];
+  double2* tile = sm;                 // [nom][32]
+  double2* cs = sm + (size_t)nom * 32;  // [nok][nom] column-major C(nom x nok)
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  for (int k = threadIdx.x; k < nom * nok; k += blockDim.x) cs[k] = C[k];
+  for (int k = threadIdx.x; k < nom * 32; k += blockDim.x) {
+    const int col = k / 32, r = k % 32;
+    const int64_t i = r0 + r;
+    double2 v = make_double2(0.0, 0.0);
+    if (i < n) {
+      const T a = V[(int64_t)col * ldv + i];
+      v = make_double2((double)a.x, (double)a.y);
+    }
+    tile[k] = v;
+  }
+  __syncthreads();
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;  // 8 column groups
+  const int64_t i = r0 + r;
+  if (i < n) {
+    for (int oc = g; oc < nok; oc += 8) {
+      double re = 0.0, im = 0.0;
+      for (int j = 0; j < nom; ++j) {
+        const double2 a = tile[j * 32 + r], c = cs[(size_t)oc * nom + j];
+        re = fma(a.x, c.x, fma(-a.y, c.y, re));
+        im = fma(a.x, c.y, fma(a.y, c.x, im));
+      }
+      T o;
+      o.x = (decltype(o.x))re;
+      o.y = (decltype(o.y))im;
+      V[(int64_t)oc * ldv + i] = o;
+    }
+  }
+}
+
+template <class T>
+__global__ void k_copy_conv(T* __restrict__ y, const double2* __restrict__ x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T o;
+    o.x = (decltype(o.x))x[i].x;
+    o.y = (decltype(o.y))x[i].y;
+    y[i] = o;
+  }
+}
+
+__global__ void k_f32_to_f64(double2* __restrict__ y, const float2* __restrict__ x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = make_double2((double)x[i].x, (double)x[i].y);
+}
+
+// Seeded start vector: psi(l) = (u_{2l} - 0.5, u_{2l+1} - 0.5), u_k = mix64(seed + (k+1)*golden)
+// >> 11 * 2^-53 (SplitMix64 finaliser), replacing random_number at eigen_solver.f90:92-96.
+__device__ __forceinline__ double su(uint64_t seed, uint64_t k) {
+  uint64_t z = seed + (k + 1ull) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return (double)(z >> 11) * 0x1.0p-53;
+}
+template <class T>
+__global__ void k_random_start(T* x, int64_t n, uint64_t seed) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T o;
+    o.x = (decltype(o.x))(su(seed, 2 * (uint64_t)i) - 0.5);
+    o.y = (decltype(o.y))(su(seed, 2 * (uint64_t)i + 1) - 0.5);
+    x[i] = o;
+  }
+}
+
+// w = q - e * v  (residual), FP64
+__global__ void k_residual(double2* __restrict__ w, const double2* __restrict__ q, const double2* __restrict__ v,
+                           int64_t n, double e) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = make_double2(q[i].x - e * v[i].x, q[i].y - e * v[i].y);
+}
+
+unsigned stream_grid(int64_t n) {
+  const int64_t g = (n + 255) / 256;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+}  // namespace
+
+// ================================================================ Vec ops
+template <class T>
+void Ops<T>::dot(const T* x, const T* y, int64_t n, double2* out) {
+  k_dot_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
+  check_launch("k_dot_part");
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 0);
+  check_launch("k_red_final");
+}
+template <class T>
+void Ops<T>::nrm(const T* x, int64_t n, double2* out) {
+  k_nrm_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
+  check_launch("k_nrm_part");
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 1);
+  check_launch("k_red_final");
+}
+template <class T>
+void Ops<T>::scale_inv(T* x, int64_t n, const double2* s) {
+  k_scale_inv<T><<<stream_grid(n), 256, 0, st>>>(x, n, s);
+  check_launch("k_scale_inv");
+}
+template <class T>
+void Ops<T>::lanczos_w(T* w, const T* q, const T* v, const T* u, int64_t n, const double2* a, const double2* b,
+                       bool real_alpha) {
+  k_lanczos_w<T><<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
+  check_launch("k_lanczos_w");
+}
+template <class T>
+void Ops<T>::axpy(T* y, const T* x, int64_t n, const double2* a, double sgn) {
+  k_axpy<T><<<stream_grid(n), 256, 0, st>>>(y, x, n, a, sgn);
+  check_launch("k_axpy");
+}
+template <class T>
+void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov) {
+  if (ncols <= 0) return;
+  k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+  check_launch("k_gemv_h_part");
+  k_gemv_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, ncols, ov);
+  check_launch("k_gemv_final");
+  k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, ov, w, n);
+  check_launch("k_gemv_sub");
+}
+template <class T>
+void Ops<T>::gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n) {
+  if (ncols <= 0) return;
+  k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  check_launch("k_gemv_sub");
+}
+template <class T>
+void Ops<T>::restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int64_t n) {
+  const size_t sm = ((size_t)nom * 32 + (size_t)nom * nok) * sizeof(double2);
+  if (sm > 48 * 1024)
+    QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_restart<T><<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+  check_launch("k_restart");
+}
+template <class T>
+void Ops<T>::random_start(T* x, int64_t n, uint64_t seed) {
+  k_random_start<T><<<stream_grid(n), 256, 0, st>>>(x, n, seed);
+  check_launch("k_random_start");
+}
+template <class T>
+void Ops<T>::from64(T* y, const double2* x, int64_t n) {
+  k_copy_conv<T><<<stream_grid(n), 256, 0, st>>>(y, x, n);
+  check_launch("k_copy_conv");
+}
+template struct Ops<double2>;
+template struct Ops<float2>;
+
+void f32_to_f64(double2* y, const float2* x, int64_t n, cudaStream_t st) {
+  k_f32_to_f64<<<stream_grid(n), 256, 0, st>>>(y, x, n);
+  check_launch("k_f32_to_f64");
+}
+void residual64(double2* w, const double2* q, const double2* v, int64_t n, double e, cudaStream_t st) {
+  k_residual<<<stream_grid(n), 256, 0, st>>>(w, q, v, n, e);
+  check_launch("k_residual");
+}
+
+// ================================================================ continued fraction
+namespace {
+// DSFLan (source_DSFLan/main.f90:52-84) for every (omega, q) pair.
+__global__ void k_cfrac(int nq, int ldab, const int* __restrict__ nlev, const double* __restrict__ alpha,
+                        const double* __restrict__ beta, const double* __restrict__ norm1,
+                        const double* __restrict__ E0, double eta, int nomega, const double* __restrict__ omega,
+                        int compat, double* __restrict__ S) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nq * nomega) return;
+  const int q = (int)(t / nomega), o = (int)(t % nomega);
+  const double* al = alpha + (size_t)q * ldab;
+  const double* be = beta + (size_t)q * ldab;
+  const int N = nlev[q];
+  const double w = omega[o], e0 = E0[q];
+  int n = N;
+  double kr = w + e0 - al[n - 1] - 0.0;
+  double bunbo = kr * kr + eta * eta;
+  double tr = be[n - 1] * kr / bunbo;
+  double ti = compat ? -be[n - 1] * eta : -be[n - 1] * eta / bunbo;
+  for (n = N - 1; n >= 2; --n) {
+    kr = w + e0 - al[n - 1] - tr;
+    const double ki = eta - ti;
+    bunbo = kr * kr + ki * ki;
+    tr = be[n - 1] * kr / bunbo;
+    ti = -be[n - 1] * ki / bunbo;
+  }
+  kr = w + e0 - al[0] - tr;
+  const double ki = eta - ti;
+  bunbo = kr * kr + ki * ki;
+  ti = -norm1[q] * ki / bunbo;
+  S[(size_t)q * nomega + o] = -ti / 3.14159265358979323846;
+}
+}  // namespace
+
+void cfrac(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,
+           const double* E0, double eta, int nomega, const double* omega, int compat, double* S, cudaStream_t st) {
+  for (int q = 0; q < nq; ++q) QS3G_REQUIRE(nlev[q] >= 1 && nlev[q] <= ldab, QS3G_EINVAL, "nlev out of range");
+  DevBuf<int> d_nlev(nq);
+  DevBuf<double> d_a((size_t)ldab * nq), d_b((size_t)ldab * nq), d_n(nq), d_e(nq), d_w(nomega),
+      d_S((size_t)nomega * nq);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_nlev.get(), nlev, nq * 4, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_a.get(), alpha, (size_t)ldab * nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_b.get(), beta2, (size_t)ldab * nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_n.get(), norm1, nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_e.get(), E0, nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_w.get(), omega, (size_t)nomega * 8, cudaMemcpyHostToDevice, st));
+  const int64_t tot = (int64_t)nq * nomega;
+  k_cfrac<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(nq, ldab, d_nlev.get(), d_a.get(), d_b.get(), d_n.get(),
+                                                        d_e.get(), eta, nomega, d_w.get(), compat, d_S.get());
+  check_launch("k_cfrac");
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(S, d_S.get(), (size_t)nomega * nq * 8, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+// ================================================================ thick-restart Lanczos
+namespace {
+
+template <class T>
+struct HvOp;
+template <>
+struct HvOp<double2> {
+  static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
+    hv64(m, s, x, y, st);
+  }
+};
+template <>
+struct HvOp<float2> {
+  static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st) {
+    hv32(m, s, x, y, st);
+  }
+};
+
+struct TrlanOut {
+  std::vector<double> ene;
+  int hv_count = 0;
+  bool converged = false;
+  int restarts = 0;
+};
+
+// lancz_eigen_val_complex (eigen_solver.f90:69-261) on device vectors of type T.
+// V must hold NOM+1 columns of length ldv; V[:,0] holds the start vector.
+template <class T>
+TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
+                    double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes) {
+  const int64_t D = s.D;
+  Ops<T> ops{st, sc.part.get()};
+  double2* alpha = sc.scal;              // [NOM+2]
+  double2* beta = sc.scal + (NOM + 2);   // [NOM+2]
+  double2* ov = sc.scal + 2 * (NOM + 2); // [NOM+2]
+  double2* cb = sc.scal + 3 * (NOM + 2); // arrow couplings [NOM+2]
+  TrlanOut out;
+  auto col = [&](int j) { return V + (int64_t)j * ldv; };
+  auto reorth = [&](int i) {  // against Fortran columns 1..i-1 = V[:, 0..i-2]
+    for (int p = 0; p < reorth_passes; ++p) ops.reorth(V, ldv, i - 1, col(i), D, ov);
+  };
+
+  // ---- initial Lanczos pass (eigen_solver.f90:98-124)
+  ops.nrm(col(0), D, beta + 0);
+  for (int i = 1; i <= NOM; ++i) {
+    ops.scale_inv(col(i - 1), D, beta + (i - 1));
+    HvOp<T>::apply(m, s, col(i - 1), Q, st);
+    ++out.hv_count;
+    ops.dot(col(i - 1), Q, D, alpha + i);
+    if (i > 1) {
+      ops.lanczos_w(col(i), Q, col(i - 1), col(i - 2), D, alpha + i, beta + (i - 1), true);
+      reorth(i);
+    } else {
+      ops.lanczos_w(col(i), Q, col(i - 1), nullptr, D, alpha + i, beta, true);
+    }
+    ops.nrm(col(i), D, beta + i);
+  }
+  ops.scale_inv(col(NOM), D, beta + NOM);
+  std::vector<double2> ha(NOM + 2), hb(NOM + 2);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(ha.data(), alpha, (NOM + 2) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(hb.data(), beta, (NOM + 2) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i <= NOM; ++i)
+    QS3G_REQUIRE(std::isfinite(hb[i].x) && hb[i].x > 0.0 && std::isfinite(ha[i < 1 ? 1 : i].x),
+                 QS3G_EBREAKDOWN, "Lanczos breakdown in the initial pass");
+  // dstevx('V','A') on the NOM x NOM tridiagonal
+  std::vector<zd> Tm((size_t)NOM * NOM, zd(0.0, 0.0));
+  for (int j = 0; j < NOM; ++j) Tm[j + (size_t)j * NOM] = ha[j + 1].x;
+  for (int j = 0; j < NOM - 1; ++j) Tm[j + (size_t)(j + 1) * NOM] = hb[j + 1].x;
+  std::vector<double> ene;
+  std::vector<zd> Cc;
+  herm_jacobi(NOM, Tm, ene, Cc);
+  std::vector<zd> calpha(NOM + 1), cbeta(NOM + 1);
+  for (int j = 1; j <= NOM; ++j) calpha[j] = ha[j].x;
+  for (int j = 0; j <= NOM; ++j) cbeta[j] = hb[j].x;
+  int flag = 0;
+  std::vector<double2> hC((size_t)NOM * NOK);
+  for (int tritr = 1; tritr <= maxitr; ++tritr) {
+    out.restarts = tritr;
+    for (int j = 0; j < NOK; ++j)
+      for (int i = 0; i < NOM; ++i) hC[(size_t)j * NOM + i] = make_double2(Cc[i + (size_t)j * NOM].real(), Cc[i + (size_t)j * NOM].imag());
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, hC.data(), hC.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
+    ops.restart(V, ldv, NOM, NOK, sc.C, D);
+    // convergence (eigen_solver.f90:150-159) or the Ritz residual bound
+    double max_conv = 0.0;
+    if (conv_mode == 0) {
+      for (int j = 0; j < NOK; ++j) max_conv = std::max(max_conv, std::abs(calpha[j + 1] / ene[j] - 1.0));
+    } else {
+      for (int j = 0; j < NOE; ++j) {
+        double rj = std::abs(cbeta[NOM] * Cc[(NOM - 1) + (size_t)j * NOM]);
+        if (conv_mode == 2) rj /= std::max(1.0, std::fabs(ene[j]));
+        max_conv = std::max(max_conv, rj);
+      }
+    }
+    flag = (max_conv < tol) ? flag + 1 : 0;
+    if ((conv_mode == 0 && flag == 2) || (conv_mode != 0 && flag >= 1)) {
+      out.converged = true;
+      break;
+    }
+    if (tritr == maxitr) break;
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(col(NOK), col(NOM), D * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    for (int j = 0; j < NOK; ++j) calpha[j + 1] = ene[j];
+    for (int j = 1; j <= NOK; ++j) cbeta[j] = cbeta[NOM] * Cc[(NOM - 1) + (size_t)(j - 1) * NOM];
+    std::vector<double2> hcb(NOK);
+    for (int j = 0; j < NOK; ++j) hcb[j] = make_double2(cbeta[j + 1].real(), cbeta[j + 1].imag());
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(cb, hcb.data(), NOK * sizeof(double2), cudaMemcpyHostToDevice, st));
+    int i = NOK + 1;
+    HvOp<T>::apply(m, s, col(i - 1), Q, st);
+    ++out.hv_count;
+    ops.dot(col(i - 1), Q, D, alpha + i);
+    ops.gemv_sub(V, ldv, NOK, cb, Q, D);
+    ops.lanczos_w(col(i), Q, col(i - 1), nullptr, D, alpha + i, beta, false);
+    reorth(i);
+    ops.nrm(col(i), D, beta + i);
+    for (i = NOK + 2; i <= NOM; ++i) {
+      ops.scale_inv(col(i - 1), D, beta + (i - 1));
+      HvOp<T>::apply(m, s, col(i - 1), Q, st);
+      ++out.hv_count;
+      ops.dot(col(i - 1), Q, D, alpha + i);
+      ops.lanczos_w(col(i), Q, col(i - 1), col(i - 2), D, alpha + i, beta + (i - 1), false);
+      reorth(i);
+      ops.nrm(col(i), D, beta + i);
+    }
+    ops.scale_inv(col(NOM), D, beta + NOM);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(ha.data(), alpha, (NOM + 2) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(hb.data(), beta, (NOM + 2) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+    for (int j = NOK + 1; j <= NOM; ++j) {
+      calpha[j] = zd(ha[j].x, ha[j].y);
+      cbeta[j] = hb[j].x;
+      QS3G_REQUIRE(std::isfinite(hb[j].x) && hb[j].x > 0.0 && std::isfinite(ha[j].x), QS3G_EBREAKDOWN,
+                   "Lanczos breakdown after a restart");
+    }
+    std::fill(Tm.begin(), Tm.end(), zd(0.0, 0.0));
+    for (int j = 0; j < NOM; ++j) Tm[j + (size_t)j * NOM] = calpha[j + 1];
+    for (int j = 0; j < NOK; ++j) Tm[j + (size_t)NOK * NOM] = cbeta[j + 1];
+    for (int j = NOK + 1; j <= NOM - 1; ++j) Tm[(j - 1) + (size_t)j * NOM] = cbeta[j];
+    herm_jacobi(NOM, Tm, ene, Cc);
+  }
+  out.ene = ene;
+  return out;
+}
+
+}  // namespace
+
+void Scratch::ensure(int nom) {
+  if (part.n == 0) part.alloc((size_t)kRedBlocks * 128);
+  if ((int)scal.n < 4 * (nom + 2)) scal.alloc(4 * (size_t)(nom + 2));
+  if ((int)C.n < nom * nom) C.alloc((size_t)nom * nom);
+}
+
+int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
+          double2* h_psi, int* iters, double* resid, cudaStream_t st) {
+  int NOM = p.NOM;
+  const int NOE = p.NOE, NOK = p.NOK;
+  QS3G_REQUIRE(NOE >= 1 && NOK >= 1 && NOE <= NOK, QS3G_EINVAL, "need 1 <= NOE <= NOK");
+  if (NOM < 2 * NOK) NOM = 2 * NOK;  // eigen_solver.f90:20
+  const int64_t D = s.D;
+  QS3G_REQUIRE(D >= NOE && D >= NOK && D >= NOM, QS3G_EINVAL, "sector dimension smaller than NOM (stop 999)");
+  QS3G_REQUIRE(NOM <= 120, QS3G_EINVAL, "NOM must be <= 120");
+  const int64_t ldv = (D + 31) / 32 * 32;
+  Scratch sc;
+  sc.ensure(NOM);
+  int hv_total = 0;
+  std::vector<double> ene;
+  DevBuf<double2> d_start;
+  const double2* start64 = nullptr;
+  if (h_start) {
+    d_start.alloc(D);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(d_start.get(), h_start, D * sizeof(double2), cudaMemcpyHostToDevice, st));
+    start64 = d_start.get();
+  }
+  bool converged = false;
+  DevBuf<double2> V64((size_t)ldv * (NOM + 1)), Q64(D);
+  if (p.precision == 1) {
+    // phase 1: complex(4) Krylov storage, FP64 reductions and Ritz solve
+    DevBuf<float2> V32((size_t)ldv * (NOM + 1)), Q32(D);
+    Ops<float2> o32{st, sc.part.get()};
+    if (start64) o32.from64(V32.get(), start64, D);
+    else o32.random_start(V32.get(), D, p.seed);
+    const double tol1 = p.tol32 > 0 ? p.tol32 : 1e-5;
+    TrlanOut r1 = trlan_core<float2>(m, s, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, st, sc,
+                                     p.reorth_passes);
+    hv_total += r1.hv_count;
+    // phase 2 start: sum of the NOE Ritz vectors, widened to FP64
+    Ops<double2> o64{st, sc.part.get()};
+    f32_to_f64(V64.get(), V32.get(), D, st);
+    for (int j = 1; j < NOE; ++j) {
+      f32_to_f64(Q64.get(), V32.get() + (int64_t)j * ldv, D, st);
+      std::vector<double2> one(1, make_double2(1.0, 0.0));
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, one.data(), sizeof(double2), cudaMemcpyHostToDevice, st));
+      o64.axpy(V64.get(), Q64.get(), D, sc.C, 1.0);
+    }
+  } else {
+    Ops<double2> o64{st, sc.part.get()};
+    if (start64) QS3G_CHECK_CUDA(cudaMemcpyAsync(V64.get(), start64, D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    else o64.random_start(V64.get(), D, p.seed);
+  }
+  TrlanOut r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, p.tol, p.conv_mode,
+                                    st, sc, p.reorth_passes);
+  hv_total += r2.hv_count;
+  converged = r2.converged;
+  ene = r2.ene;
+  for (int j = 0; j < NOE; ++j) ene_out[j] = ene[j];
+  if (iters) *iters = hv_total;
+  // FP64 residuals ||H psi_j - E_j psi_j|| of the Ritz vectors in V[:, :NOE]
+  if (resid || h_psi) {
+    Ops<double2> o64{st, sc.part.get()};
+    DevBuf<double2> W(D);
+    for (int j = 0; j < NOE; ++j) {
+      double2* pj = V64.get() + (int64_t)j * ldv;
+      if (resid) {
+        hv64(m, s, pj, Q64.get(), st);
+        residual64(W.get(), Q64.get(), pj, D, ene[j], st);
+        o64.nrm(W.get(), D, sc.scal);
+        double2 r;
+        QS3G_CHECK_CUDA(cudaMemcpyAsync(&r, sc.scal, sizeof(double2), cudaMemcpyDeviceToHost, st));
+        QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+        resid[j] = r.x;
+      }
+      if (h_psi)
+        QS3G_CHECK_CUDA(cudaMemcpyAsync(h_psi + (int64_t)j * D, pj, D * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
+  return converged ? QS3G_OK : QS3G_ENOTCONV;
+}
+
+// ================================================================ plain Lanczos (ALG=1)
+int lanczos(const Model& m, const Sector& s, int maxitr, int minitr, int itrint, double tol, const double2* h_start,
+            uint64_t seed, double* ene_out, double2* h_psi, int* iters, cudaStream_t st) {
+  const int64_t D = s.D;
+  QS3G_REQUIRE(D >= 1, QS3G_ESTATE, "empty sector");
+  QS3G_REQUIRE(maxitr >= 1 && itrint >= 1, QS3G_EINVAL, "maxitr, itrint must be >= 1");
+  Scratch sc;
+  sc.ensure(8);
+  Ops<double2> ops{st, sc.part.get()};
+  DevBuf<double2> v1(D), v2(D), v3(D), io(D);
+  DevBuf<double2> d_ab((size_t)2 * (maxitr + 2));  // alpha[i], beta[i] as double2
+  double2* alpha = d_ab.get();
+  double2* beta = d_ab.get() + (maxitr + 2);
+  if (h_start) QS3G_CHECK_CUDA(cudaMemcpyAsync(v1.get(), h_start, D * sizeof(double2), cudaMemcpyHostToDevice, st));
+  else ops.random_start(v1.get(), D, seed);
+  ops.nrm(v1.get(), D, beta + 0);
+  ops.scale_inv(v1.get(), D, beta + 0);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(io.get(), v1.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  const int mitr = (int)std::min<int64_t>(maxitr, D);
+  double tmp = 0.0, ene = 0.0;
+  std::vector<double> z;
+  int ite = -1;
+  std::vector<double2> ha, hb;
+  for (int i = 1; i <= mitr; ++i) {
+    hv64(m, s, v1.get(), v2.get(), st);
+    ops.dot(v1.get(), v2.get(), D, alpha + i);
+    if (i > 1) ops.lanczos_w(v2.get(), v2.get(), v1.get(), v3.get(), D, alpha + i, beta + (i - 1), true);
+    else ops.lanczos_w(v2.get(), v2.get(), v1.get(), nullptr, D, alpha + i, beta, true);
+    ops.nrm(v2.get(), D, beta + i);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v3.get(), v1.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v1.get(), v2.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    ops.scale_inv(v1.get(), D, beta + i);
+    if (i == mitr || (i >= minitr && i % itrint == 0)) {
+      ha.resize(i + 1);
+      hb.resize(i + 1);
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(ha.data(), alpha, (i + 1) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(hb.data(), beta, (i + 1) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (i == 1) {  // lanczos.f90:99-106
+        ene_out[0] = ha[1].x;
+        if (h_psi) {
+          std::vector<double2> e(D, make_double2(0.0, 0.0));
+          e[0] = make_double2(1.0, 0.0);
+          std::memcpy(h_psi, e.data(), D * sizeof(double2));
+        }
+        if (iters) *iters = 1;
+        return QS3G_OK;
+      }
+      std::vector<double> d(i), e(i - 1);
+      for (int k = 0; k < i; ++k) d[k] = ha[k + 1].x;
+      for (int k = 0; k < i - 1; ++k) e[k] = hb[k + 1].x;
+      tridiag_lowest(d, e, ene, z);
+      const double conv = std::fabs(tmp / ene - 1.0);
+      if (i == maxitr || conv < tol) { ite = i; break; }
+      tmp = ene;
+    }
+  }
+  QS3G_REQUIRE(ite > 0, QS3G_ENOTCONV, "Lanczos reached min(maxitr, dim) without converging");
+  ene_out[0] = ene;
+  if (iters) *iters = 2 * ite - 1;
+  if (!h_psi) return QS3G_OK;
+  // eigenvector replay (lanczos.f90:123-150)
+  std::vector<double2> hz(ite);
+  for (int k = 0; k < ite; ++k) hz[k] = make_double2(z[k], 0.0);
+  DevBuf<double2> dz(ite);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(dz.get(), hz.data(), ite * sizeof(double2), cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(v1.get(), io.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  // psi_io = z(1) * psi_io  (my_zdscal)
+  QS3G_CHECK_CUDA(cudaMemsetAsync(io.get(), 0, D * sizeof(double2), st));
+  ops.axpy(io.get(), v1.get(), D, dz.get(), 1.0);
+  for (int i = 1; i <= ite - 1; ++i) {
+    hv64(m, s, v1.get(), v2.get(), st);
+    if (i > 1) ops.lanczos_w(v2.get(), v2.get(), v1.get(), v3.get(), D, alpha + i, beta + (i - 1), true);
+    else ops.lanczos_w(v2.get(), v2.get(), v1.get(), nullptr, D, alpha + i, beta, true);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v3.get(), v1.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v1.get(), v2.get(), D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    ops.scale_inv(v1.get(), D, beta + i);
+    ops.axpy(io.get(), v1.get(), D, dz.get() + i, 1.0);
+  }
+  ops.nrm(io.get(), D, beta + 0);
+  ops.scale_inv(io.get(), D, beta + 0);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(h_psi, io.get(), D * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  return QS3G_OK;
+}
+
+}  // namespace qs3g

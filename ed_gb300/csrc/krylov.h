@@ -1,0 +1,68 @@
+// krylov.h -- host wrappers of the level-1 kernels and the Krylov drivers.
+#pragma once
+
+#include "qs3g_internal.cuh"
+
+namespace qs3g {
+
+constexpr int kRedBlocks = 152 * 4;  // fixed reduction grid: 4 blocks per SM of the GB300
+
+// Device scratch of one solve: reduction partials, Lanczos scalars, Ritz coefficients.
+struct Scratch {
+  DevBuf<double2> part;  // kRedBlocks x (up to 128 columns)
+  DevBuf<double2> scal;  // alpha, beta, overlaps, arrow couplings
+  DevBuf<double2> C;     // NOM x NOK Ritz coefficients
+  void ensure(int nom);
+};
+
+// Level-1 operations on vectors of T (double2 = complex(8), float2 = complex(4));
+// every reduction accumulates in FP64 and writes its result to device memory.
+template <class T>
+struct Ops {
+  cudaStream_t st;
+  double2* part;
+  void dot(const T* x, const T* y, int64_t n, double2* out);              // zdotc
+  void nrm(const T* x, int64_t n, double2* out);                          // dznrm2 -> out->x
+  void scale_inv(T* x, int64_t n, const double2* s);                      // x *= 1/s->x
+  void lanczos_w(T* w, const T* q, const T* v, const T* u, int64_t n, const double2* a, const double2* b,
+                 bool real_alpha);                                        // w = q - a v - b u
+  void axpy(T* y, const T* x, int64_t n, const double2* a, double sgn);    // y += sgn*a*x
+  void reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov);  // w -= V V^H w
+  void gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n);
+  void restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int64_t n);
+  void random_start(T* x, int64_t n, uint64_t seed);
+  void from64(T* y, const double2* x, int64_t n);
+};
+
+void f32_to_f64(double2* y, const float2* x, int64_t n, cudaStream_t st);
+void residual64(double2* w, const double2* q, const double2* v, int64_t n, double e, cudaStream_t st);
+
+struct TrlanParams {
+  int NOE = 1, NOK = 2, NOM = 4, maxitr = 1000;
+  double tol = 1e-12;
+  int precision = 0;      // 0 complex(8), 1 complex(4) storage + FP64 refinement
+  int conv_mode = 0;      // 0 reference, 1 residual <= tol, 2 residual <= tol*max(1,|E|)
+  uint64_t seed = 1;
+  double tol32 = 0.0;     // phase-1 relative residual target (0: default 1e-5)
+  int reorth_passes = 1;
+};
+
+int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
+          double2* h_psi, int* iters, double* resid, cudaStream_t st);
+int lanczos(const Model& m, const Sector& s, int maxitr, int minitr, int itrint, double tol, const double2* h_start,
+            uint64_t seed, double* ene_out, double2* h_psi, int* iters, cudaStream_t st);
+void cfrac(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,
+           const double* E0, double eta, int nomega, const double* omega, int compat, double* S, cudaStream_t st);
+
+// DSF (calcu_Sq_a + calcu_DSF_wavevector) for nq wave vectors.
+int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int spsmsz, int nq, const double* qvec,
+        const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2, double* norm1, double* E0,
+        int* nlev, cudaStream_t st);
+
+// Sector build for an arbitrary wave vector rk (DSF sectors use rk + q).
+void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cudaStream_t st);
+
+int64_t connection_table_rows(const Model& m, const Sector& s, int64_t row0, int64_t row1, int64_t* row,
+                              int64_t* col, int* ell, int* bond, int64_t cap, cudaStream_t st);
+
+}  // namespace qs3g

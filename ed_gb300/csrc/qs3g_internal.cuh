@@ -1,0 +1,157 @@
+// qs3g_internal.cuh -- shared declarations of the GB300 QS3 hot-path library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/qs3g.h"
+
+namespace qs3g {
+
+// ---------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define QS3G_CHECK_CUDA(call)                                                          \
+  do {                                                                                 \
+    cudaError_t _e = (call);                                                           \
+    if (_e != cudaSuccess)                                                             \
+      throw ::qs3g::Error(_e == cudaErrorMemoryAllocation ? QS3G_ENOMEM : QS3G_ECUDA,  \
+                          std::string(#call) + ": " + cudaGetErrorString(_e));         \
+  } while (0)
+
+#define QS3G_REQUIRE(cond, code, msg)                        \
+  do {                                                       \
+    if (!(cond)) throw ::qs3g::Error((code), (msg));         \
+  } while (0)
+
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+inline void check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(QS3G_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  count_launch();
+}
+
+// ---------------------------------------------------------------- device buffers
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    QS3G_CHECK_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  T* get() const { return p; }
+  operator T*() const { return p; }
+};
+
+// ---------------------------------------------------------------- limits
+constexpr int kMaxNOD = 8;          // template instantiations of the row kernels
+constexpr int kDirBits = 224;       // candidates per 32-byte directory block
+constexpr int kDirWords = 8;        // base (1 word) + 7 bit words
+
+// ---------------------------------------------------------------- model
+// Lattice + bonds as read by read_ip (input_param.f90:58-117).
+struct Model {
+  int NOS = 0, LX = 0, LY = 0, LZ = 0, NOxxz = 0;
+  bool chain = false;               // LY == LZ == 1: one translation axis
+  int bits = 0;                     // bits per site in a packed configuration
+  std::vector<int> p1, p2;          // bond ends (1-based, p1 <= p2)
+  std::vector<double> sJxy, sJz;    // sJint(:,2), sJint(:,3)
+  double Sz_all = 0.0;              // sum_b sJz_b
+  // per-site adjacency of non-self bonds: entries (neighbour, bond), both ends listed
+  std::vector<int> adj_off;         // NOS + 2 (index by site 1..NOS, [NOS+1] end)
+  std::vector<uint32_t> adj;        // packed (bond << 16) | neighbour  (NOS < 65536, bonds < 65536)
+  std::vector<double> Sz_site;      // sum of sJz over the non-self bonds at a site (index 1..NOS)
+  // device copies
+  DevBuf<int> d_adj_off;
+  DevBuf<uint32_t> d_adj;
+  DevBuf<double> d_sJxy, d_sJz, d_Sz_site;
+  DevBuf<int16_t> d_site_xyz;       // (x, y, z, pad) 0-based per site, index 1..NOS
+};
+
+// ---------------------------------------------------------------- sector
+// A (NOD, K) representative basis (allocate_lists_omp_SQ, state_lists.f90:225-292).
+struct Sector {
+  int NOD = 0;
+  int K[3] = {0, 0, 0};
+  double rk[3] = {0, 0, 0};
+  bool anchored = false;            // chain: reps occupy site 1, directory over C(NOS-1, NOD-1)
+  bool kzero = false;               // every phase equals exp(0) = 1 exactly
+  uint64_t nspace = 0;              // candidates in the directory space
+  int64_t D = 0;
+  uint64_t nblocks = 0;             // directory blocks
+  DevBuf<int64_t> d_list_s;         // colex ranks (1-based), ascending
+  DevBuf<double> d_list_r;          // sqrt(norm^2)
+  DevBuf<float> d_list_r32;         // float copy for the complex(4) kernels
+  DevBuf<uint64_t> d_conf;          // packed sorted down-spin sites
+  DevBuf<uint32_t> d_dir;           // nblocks x 8 words: base row, 224 presence bits
+  DevBuf<double2> d_explist;        // explist(0:LX,0:LY,0:LZ), Fortran order
+  DevBuf<double2> d_chainph;        // chain: explist(i,1,1) for i = 1..LX, [0] = explist(0,0,0)
+  DevBuf<float2> d_chainph32;
+  DevBuf<uint64_t> d_binom;         // C(n,k) for n in [0,NOS], k in [0,NOD+1]: [k*(NOS+1)+n]
+  DevBuf<uint32_t> d_binomA;        // anchored: C(x,k) for x in [0,NOS-2], k in [1,NOD-1] (u32)
+};
+
+// Host-side explist (input_param.f90:87-89) and checkstate phases
+// (state_lists.f90:84-104), computed with the host libm exactly as the
+// Fortran expressions are written.
+void wavevector(const int K[3], int LX, int LY, int LZ, double rk[3]);
+void host_explist(const double rk[3], int LX, int LY, int LZ, std::vector<double2>& out);
+
+// ---------------------------------------------------------------- kernels (host wrappers)
+void build_sector(const Model& m, int NOD, const int K[3], Sector& s, cudaStream_t st);
+
+struct HvWork {  // scratch for the general-lattice kernel (none needed today)
+};
+
+void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st);
+void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+
+// connection table: counts per row then entries
+int64_t connection_table(const Model& m, const Sector& s, int64_t* row, int64_t* col, int* ell,
+                         int* bond, int64_t cap, cudaStream_t st);
+
+// Binomial helper on host (64-bit, saturating at INT64_MAX).
+uint64_t binom_u64(int n, int k);
+int bits_for(int v);
+
+}  // namespace qs3g
+
+// the opaque handle
+struct qs3g_ctx {
+  qs3g::Model model;
+  std::unique_ptr<qs3g::Sector> sector;
+  cudaStream_t stream = nullptr;
+  bool own_stream = true;
+  qs3g::DevBuf<char> stage[2];  // device staging of the host-pointer H*v forms
+  std::string last_error;
+};

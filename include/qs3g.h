@@ -1,0 +1,162 @@
+/* qs3g.h -- C ABI of libqs3g.so, the GB300 (sm_103a) implementation of the
+ * QS3 matrix-free Lanczos hot path.
+ *
+ * Every entry point is extern "C", takes scalars by pointer so that a Fortran
+ * `bind(C)` interface can pass them by reference, and returns an int status
+ * (QS3G_OK = 0).  No C++ exception crosses this boundary.  Row and site
+ * numbers at the boundary are 1-based as in the Fortran; `qs3g_cplx` has the
+ * layout of Fortran complex(8); arrays are column-major where they have two
+ * dimensions.  One handle belongs to one host thread and owns one CUDA
+ * stream; calls on the same handle are not re-entrant.
+ *
+ * Reference interfaces each entry point replaces are cited as
+ * path:line within the QS-Cube/ED source tree.
+ */
+#ifndef QS3G_H
+#define QS3G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qs3g_ctx* qs3g_handle;
+typedef struct { double re, im; } qs3g_cplx;   /* complex(8) */
+typedef struct { float re, im; } qs3g_cplx32;  /* complex(4) */
+
+enum {
+  QS3G_OK = 0,
+  QS3G_EINVAL = 1,     /* bad argument (the Fortran would `stop`) */
+  QS3G_ENOMEM = 2,     /* device allocation failed */
+  QS3G_ENOTCONV = 3,   /* solver stopped at its iteration cap without converging */
+  QS3G_EITERCAP = 4,   /* a device loop hit its iteration cap */
+  QS3G_ECUDA = 5,      /* CUDA runtime error */
+  QS3G_ESTATE = 6,     /* call out of order (e.g. no sector built) */
+  QS3G_ERANGE = 7,     /* sizes beyond what the kernels index (64-bit ranks, packed sites) */
+  QS3G_ENOTSUP = 8,    /* option not implemented for this lattice */
+  QS3G_EBREAKDOWN = 9  /* Lanczos breakdown (beta = 0) or non-finite value */
+};
+
+/* Location of vector arguments. */
+enum { QS3G_HOST = 0, QS3G_DEVICE = 1 };
+
+/* Create a handle for the lattice and bonds.
+ * Replaces the module state set up by read_ip (source/input_param.f90:58-117),
+ * get_combination (source/state_lists.f90:6-15) and mk_shift_{x,y,z}_SQ
+ * (source/state_lists.f90:36-64; called at source/main.f90:49-51).
+ * p_xxz is p_xxz(1:2,1:NOxxz); sJint is sJint(1:NOxxz,2:3), i.e. Jxy/2 for
+ * every bond followed by Jz/4 for every bond.  Bond ends are swapped to i<j
+ * as input_param.f90:97-101 does.  NOS must equal LX*LY*LZ. */
+int qs3g_create(qs3g_handle* h, const int* NOS, const int* LX, const int* LY, const int* LZ,
+                const int* NOxxz, const int* p_xxz, const double* sJint);
+
+/* Release the handle and all device memory it owns. */
+int qs3g_destroy(qs3g_handle h);
+
+/* Build the (NOD, K) representative basis on the GPU.
+ * Replaces allocate_lists_omp_SQ + checkstate_SQ (source/state_lists.f90:66-112,
+ * 225-292; called at source/main.f90:54) and the explist of
+ * source/input_param.f90:87-89.  D_out receives THS(k). */
+int qs3g_build_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ,
+                      int64_t* D_out);
+
+/* Copy the sector lists to the host: list_s(1:D) (colex ranks, ascending)
+ * and list_r(1:D) = sqrt(norm^2), as allocate_lists_omp_SQ leaves them. */
+int qs3g_get_sector(qs3g_handle h, int64_t* list_s, double* list_r);
+
+/* Run the handle's work on a caller-owned CUDA stream (a cudaStream_t passed
+ * as void*) instead of the handle's own stream.  No counterpart in the
+ * reference, which has no device; the analogue of cublasSetStream. */
+int qs3g_set_stream(qs3g_handle h, void* stream);
+
+/* Wait for all work queued on the handle's stream. */
+int qs3g_sync(qs3g_handle h);
+
+/* Matrix-free H*v in the current sector: v0 = H v1.
+ * Replaces ham_to_vec_wave_vector (source/ham2vec_v3.f90:37-72).
+ * where = QS3G_HOST copies v1 in and v0 out and returns when v0 is written;
+ * QS3G_DEVICE takes device pointers and queues the product on the handle's
+ * stream without waiting (call qs3g_sync before reading v0). */
+int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where);
+
+/* Same product with complex(4) vectors (FP32 Krylov storage). */
+int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* where);
+
+/* The connection table of ham_to_vec_wave_vector: one entry per antiparallel
+ * bond whose hop lands on a row of the sector (the `id > 0` branch of
+ * source/ham2vec_v3.f90:61-65): 1-based row and column, the translation
+ * ell(1:3) of representative_SQ (source/state_lists.f90:384-416), and the
+ * 1-based bond number.  Rows ascend; within a row, bonds ascend.
+ * On entry *nnz is the capacity of the arrays; on return it is the number of
+ * entries (QS3G_ERANGE if the capacity was too small; pass row == NULL to
+ * query the count). */
+int qs3g_connection_table(qs3g_handle h, int64_t* row, int64_t* col, int* ell, int* bond,
+                          int64_t* nnz);
+
+/* The same table restricted to rows row_first..row_last (1-based, inclusive),
+ * for sectors too large to tabulate at once. */
+int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const int64_t* row_last,
+                               int64_t* row, int64_t* col, int* ell, int* bond, int64_t* nnz);
+
+/* Thick-restart Lanczos for the lowest NOE eigenpairs.
+ * Replaces my_trlanczos_routines_complex + lancz_eigen_val_complex
+ * (source/eigen_solver.f90:10-49,69-261; called at source/main.f90:92).
+ * precision: 0 = complex(8) Krylov vectors; 1 = complex(4) storage with FP64
+ *            reductions, reorthogonalisation and Ritz solve, followed by an FP64
+ *            refinement phase.
+ * conv_mode: 0 = the reference's test (|E_prev/E - 1| < tol on two consecutive
+ *            restarts, eigen_solver.f90:150-159);
+ *            1 = Ritz residual |beta_NOM C(NOM,j)| <= tol for j = 1..NOE.
+ * start_mode: 0 = random start from `seed`; 1 = start vector given in `start`
+ *            (host, D elements).
+ * ene(1:NOE) receives the eigenvalues; psi (host, D x NOE column-major, may be
+ * NULL) the Ritz vectors; iters receives the number of H*v products; resid
+ * (may be NULL) receives ||H psi_j - E_j psi_j||_2 recomputed in FP64. */
+int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, const int* maxitr,
+               const double* tol, const int* precision, const int* conv_mode,
+               const int* start_mode, const uint64_t* seed, const qs3g_cplx* start, double* ene,
+               qs3g_cplx* psi, int* iters, double* resid);
+
+/* Plain Lanczos (ALG=1) for the lowest eigenpair.
+ * Replaces lanczos_routines + lancz_eigen_val (source/lanczos.f90:14-152). */
+int qs3g_lanczos(qs3g_handle h, const int* maxitr, const int* minitr, const int* itrint,
+                 const double* tol, const int* start_mode, const uint64_t* seed,
+                 const qs3g_cplx* start, double* ene, qs3g_cplx* psi, int* iters);
+
+/* Dynamical structure factor recursion for nq momentum transfers at once.
+ * Replaces calcu_Sq_a + calcu_DSF_wavevector
+ * (source/get_expectation_values.f90:281-605; called at source/main.f90:178).
+ * psi: ground state in the current sector (host, D elements); ene1: its energy
+ * (ene(1)); spsmsz: 1 = S+, 2 = S-, 3 = Sz; qvec: nq x 3 wave vectors
+ * (kvec_calc per q); Spos: site positions Spos(1:3,1:NOS); itr_dsf: number of
+ * recursion levels; rfield: Zeeman field.
+ * Outputs per q (column-major itr_dsf x nq): alpha(1:itr_dsf) and
+ * beta2(1:itr_dsf) exactly as written to alpha_beta_values_*.d (beta2(1) = 0),
+ * norm1(1:nq), E0(1:nq) = ene1 - rfield*sztot, nlev(1:nq) = levels computed. */
+int qs3g_dsf(qs3g_handle h, const qs3g_cplx* psi, const double* ene1, const int* spsmsz,
+             const int* nq, const double* qvec, const double* Spos, const int* itr_dsf,
+             const double* rfield, double* alpha, double* beta2, double* norm1, double* E0,
+             int* nlev);
+
+/* Continued fraction S(omega) = -Im G / pi of DSFLan
+ * (source_DSFLan/main.f90:52-84) for nq spectra at once on an arbitrary omega
+ * grid.  alpha/beta2 are column-major (ldab x nq) with nlev(q) levels used;
+ * compat = 1 keeps the reference's deepest level (imaginary part not divided
+ * by its denominator), compat = 0 evaluates the plain continued fraction.
+ * S is column-major (nomega x nq).  Host arrays. */
+int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* alpha,
+               const double* beta2, const double* norm1, const double* E0, const double* eta,
+               const int* nomega, const double* omega, const int* compat, double* S);
+
+/* Last error message for the handle (or the last global one if h is NULL). */
+const char* qs3g_last_error(qs3g_handle h);
+
+/* Number of kernels this library has launched since load (for accounting). */
+int64_t qs3g_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QS3G_H */

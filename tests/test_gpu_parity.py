@@ -1,0 +1,245 @@
+"""GPU parity of libqs3g.so against the CPU oracle (small and medium sectors).
+
+Every call goes through the C ABI (ed_gb300.capi).  Tolerances:
+  * list_s, connection table (row, col, ell, bond): bit-exact;
+  * list_r: 1e-15 relative (both sides use the host libm for the phases);
+  * H*v (complex(8)): max |y_gpu - y_oracle| <= 1e-13 * max |y_oracle|;
+  * H*v (complex(4)): 2e-6 relative in the same norm;
+  * eigenvalues: 1e-10 relative; DSF alpha/beta^2: 1e-8 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import dense_ed as E
+from oracle import oracle as O
+from oracle import solvers as S
+from ed_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+CHAINS = [
+    # (L, NOD, K, J1, J2)
+    (12, 3, 0, (1.0, 1.0), None),
+    (12, 4, 3, (1.0, 0.5), (0.3, 0.3)),
+    (14, 4, 7, (1.0, 0.7), (0.25, 0.1)),
+    (16, 2, 5, (-1.0, -1.0), None),
+    (18, 6, 0, (1.0, 0.5), (0.3, 0.3)),
+    (20, 5, 4, (1.0, 1.0), (0.2, 0.2)),
+    (24, 1, 6, (1.0, 0.3), None),
+    (24, 4, 12, (1.0, 2.0), (0.5, 0.5)),
+    (30, 3, 10, (1.0, 1.0), None),
+]
+
+LATTICES = [
+    # (LX, LY, LZ, NOD, K, bonds-kind)
+    (4, 3, 1, 3, (1, 2, 0), "square"),
+    (4, 4, 1, 2, (0, 0, 0), "square"),
+    (3, 3, 2, 3, (1, 0, 1), "cubic"),
+    (6, 6, 1, 3, (0, 0, 0), "square"),
+    (4, 4, 1, 4, (2, 1, 0), "triangular"),
+]
+
+
+def lattice_bonds(LX, LY, LZ, kind, rng):
+    bonds = []
+    site = lambda x, y, z: 1 + (x % LX) + LX * ((y % LY) + LY * (z % LZ))
+    for z in range(LZ):
+        for y in range(LY):
+            for x in range(LX):
+                s = site(x, y, z)
+                bonds.append((s, site(x + 1, y, z)))
+                if LY > 1:
+                    bonds.append((s, site(x, y + 1, z)))
+                if LZ > 1:
+                    bonds.append((s, site(x, y, z + 1)))
+                if kind == "triangular":
+                    bonds.append((s, site(x + 1, y + 1, z)))
+    n = len(bonds)
+    jxy = rng.uniform(0.5, 1.5, n)
+    jz = rng.uniform(-1.0, 1.0, n)
+    return np.array(bonds, np.int32), jxy, jz
+
+
+def make_chain(L, J1, J2):
+    b, jxy, jz = inputs.chain_bonds(L, J1, J2)
+    return (L, L, 1, 1, b, jxy, jz)
+
+
+def both(args, nod, K):
+    from ed_gb300 import capi
+    NOS, LX, LY, LZ, b, jxy, jz = args
+    om = O.Model(NOS, LX, LY, LZ, b, jxy, jz, kmax=min(NOS, nod + 2))
+    osec = om.build_sector(nod, K)
+    h = capi.Handle(NOS, LX, LY, LZ, b, jxy, jz)
+    D = h.build_sector(nod, K)
+    return om, osec, h, D
+
+
+def check_sector(osec, h, D):
+    assert D == osec.D
+    ls, lr = h.get_sector()
+    np.testing.assert_array_equal(ls, osec.list_s)
+    np.testing.assert_allclose(lr, osec.list_r, rtol=1e-15, atol=0)
+
+
+def check_table(osec, h):
+    r0, c0, e0, b0 = osec.connection_table()
+    r1, c1, e1, b1 = h.connection_table()
+    np.testing.assert_array_equal(r1, r0 + 1)
+    np.testing.assert_array_equal(c1, c0 + 1)
+    np.testing.assert_array_equal(e1, e0)
+    np.testing.assert_array_equal(b1, b0 + 1)
+    return len(r0)
+
+
+def check_hv(osec, h, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(osec.D) + 1j * rng.standard_normal(osec.D)
+    y0 = osec.hv(x)
+    y1 = h.hv(x)
+    scale = np.abs(y0).max()
+    assert np.abs(y1 - y0).max() <= 1e-13 * scale
+    x32 = x.astype(np.complex64)
+    y2 = h.hv32(x32)
+    y0b = osec.hv(x32.astype(np.complex128))
+    assert np.abs(y2 - y0b).max() <= 2e-6 * np.abs(y0b).max()
+
+
+@pytest.mark.parametrize("L,nod,K,J1,J2", CHAINS)
+def test_chain_sector_table_hv(qs3g, L, nod, K, J1, J2):
+    args = make_chain(L, J1, J2)
+    om, osec, h, D = both(args, nod, (K, 0, 0))
+    check_sector(osec, h, D)
+    if D:
+        check_table(osec, h)
+        check_hv(osec, h)
+    h.close()
+
+
+@pytest.mark.parametrize("LX,LY,LZ,nod,K,kind", LATTICES)
+def test_lattice_sector_table_hv(qs3g, LX, LY, LZ, nod, K, kind):
+    rng = np.random.default_rng(LX * 100 + LY * 10 + LZ)
+    b, jxy, jz = lattice_bonds(LX, LY, LZ, kind, rng)
+    args = (LX * LY * LZ, LX, LY, LZ, b, jxy, jz)
+    om, osec, h, D = both(args, nod, K)
+    check_sector(osec, h, D)
+    if D:
+        check_table(osec, h)
+        check_hv(osec, h)
+    h.close()
+
+
+def test_sector_sum_rule(qs3g):
+    """Every orbit of period p is a row of exactly p momentum sectors, so the
+    sector dimensions add up to C(L, NOD); the K = 0 sector holds every orbit,
+    so its orbit sizes p = L^2 / list_r^2 add up to C(L, NOD) as well."""
+    from ed_gb300 import capi
+    from math import comb
+    L, nod = 20, 4
+    b, jxy, jz = inputs.chain_bonds(L)
+    h = capi.Handle(L, L, 1, 1, b, jxy, jz)
+    total = 0
+    for K in range(L):
+        total += h.build_sector(nod, (K, 0, 0))
+    assert total == comb(L, nod)
+    h.build_sector(nod, (0, 0, 0))
+    ls, lr = h.get_sector()
+    assert int(np.rint(L * L / lr ** 2).sum()) == comb(L, nod)
+    h.close()
+
+
+@pytest.mark.parametrize("L,nod,K,J1,J2", [(14, 4, 0, (1.0, 0.5), (0.3, 0.3)),
+                                           (16, 3, 5, (1.0, 1.0), None),
+                                           (12, 6, 0, (1.0, 1.0), None)])
+def test_trlan_eigenvalues(qs3g, L, nod, K, J1, J2):
+    args = make_chain(L, J1, J2)
+    om, osec, h, D = both(args, nod, (K, 0, 0))
+    w = np.linalg.eigvalsh(osec.dense())
+    NOE, NOK, NOM = 4, 6, 12
+    r = h.trlan(NOE, NOK, NOM, maxitr=500, tol=1e-12, seed=11)
+    np.testing.assert_allclose(r["ene"], w[:NOE], rtol=1e-10, atol=1e-10)
+    assert r["resid"].max() < 1e-8
+    # oracle TRLan from the same seeded start vector
+    ene, _, _, conv = S.trlan(osec.hv, D, NOE, NOK, NOM, 500, 1e-12, S.start_vector(D, 11))
+    np.testing.assert_allclose(r["ene"], ene[:NOE], rtol=1e-10, atol=1e-10)
+    # FP32 storage + FP64 refinement reaches the same eigenvalues
+    r32 = h.trlan(NOE, NOK, NOM, maxitr=500, tol=1e-12, precision=1, seed=11)
+    np.testing.assert_allclose(r32["ene"], w[:NOE], rtol=1e-10, atol=1e-10)
+    # residual-based convergence
+    rr = h.trlan(1, 4, 12, maxitr=500, tol=1e-10, conv_mode=1, seed=3)
+    assert rr["resid"][0] <= 2e-10
+    assert abs(rr["ene"][0] - w[0]) <= 1e-10 * max(1.0, abs(w[0]))
+    h.close()
+
+
+def test_start_vector_matches_oracle(qs3g):
+    """The seeded start vector is generated identically on both sides."""
+    args = make_chain(10, (1.0, 1.0), None)
+    om, osec, h, D = both(args, 3, (0, 0, 0))
+    st = S.start_vector(D, 1234)
+    r1 = h.trlan(2, 3, 6, maxitr=200, tol=1e-13, seed=1234)
+    r2 = h.trlan(2, 3, 6, maxitr=200, tol=1e-13, start=st)
+    np.testing.assert_array_equal(r1["ene"], r2["ene"])
+    h.close()
+
+
+def test_lanczos(qs3g):
+    args = make_chain(16, (1.0, 0.5), (0.3, 0.3))
+    om, osec, h, D = both(args, 4, (0, 0, 0))
+    w = np.linalg.eigvalsh(osec.dense())
+    r = h.lanczos(maxitr=2000, minitr=20, itrint=5, tol=1e-14, seed=5)
+    assert abs(r["ene"] - w[0]) <= 1e-10 * abs(w[0])
+    psi = r["psi"]
+    res = np.linalg.norm(osec.hv(psi) - r["ene"] * psi)
+    assert res < 1e-6
+    e2, p2, ite = S.lanczos(osec.hv, D, 2000, 20, 5, 1e-14, S.start_vector(D, 5))
+    assert abs(r["ene"] - e2) <= 1e-10 * abs(e2)
+    h.close()
+
+
+@pytest.mark.parametrize("spsmsz", [1, 2, 3])
+def test_dsf_small(qs3g, spsmsz):
+    L, nod = 14, 3
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 1.0), None)
+    args = (L, L, 1, 1, b, jxy, jz)
+    om, osec, h, D = both(args, nod, (0, 0, 0))
+    w, V = np.linalg.eigh(osec.dense())
+    psi = V[:, 0]
+    Spos = inputs.chain_positions(L)
+    nod_new = {1: nod - 1, 2: nod + 1, 3: nod}[spsmsz]
+    qs = [2 * np.pi * m / L for m in (0, 1, 4, 7)]
+    itr = 12
+    rfield = 0.1
+    g = h.dsf(psi, w[0], spsmsz, [(q, 0, 0) for q in qs], Spos, itr, rfield)
+    for iq, q in enumerate(qs):
+        rk = O.wavevector((0, 0, 0), om.Ls) + np.array([q, 0, 0])
+        D2 = O.lib().ora_build_sector(om.h, nod_new, rk, None, None, 0, 0)
+        ls = np.zeros(D2, np.int64)
+        lr = np.zeros(D2)
+        O.lib().ora_build_sector(om.h, nod_new, rk, ls.ctypes.data, lr.ctypes.data, D2, 0)
+        ns = O.Sector(om, nod_new, (0, 0, 0), ls, lr, rk=rk)
+        fn = O.sq_a(spsmsz, osec, ns, (q, 0, 0), Spos, psi)
+        a, b2, n1, nl = S.dsf_recursion(ns.hv, fn, itr, rfield, L, nod_new)
+        assert g["nlev"][iq] == nl
+        np.testing.assert_allclose(g["norm1"][iq], n1, rtol=1e-12)
+        np.testing.assert_allclose(g["alpha"][iq, :nl], a, rtol=1e-8, atol=1e-10)
+        np.testing.assert_allclose(g["beta2"][iq, :nl], b2, rtol=1e-8, atol=1e-10)
+    h.close()
+
+
+def test_cfrac(qs3g):
+    from ed_gb300 import capi
+    rng = np.random.default_rng(4)
+    nq, N = 5, 40
+    alpha = rng.uniform(-1, 3, (nq, N))
+    beta2 = rng.uniform(0.1, 2, (nq, N))
+    beta2[:, 0] = 0.0
+    nlev = np.array([40, 30, 1, 2, 17], np.int32)
+    norm1 = rng.uniform(0.5, 2, nq)
+    E0 = rng.uniform(-5, -1, nq)
+    om = np.linspace(0, 6, 2000)
+    for compat in (True, False):
+        S1 = capi.cfrac(alpha, beta2, nlev, norm1, E0, 0.05, om, compat)
+        for q in range(nq):
+            S0 = O.cfrac(alpha[q, :nlev[q]], beta2[q, :nlev[q]], norm1[q], E0[q], 0.05, om, compat)
+            np.testing.assert_allclose(S1[q], S0, rtol=1e-12, atol=1e-14)
