@@ -59,7 +59,8 @@ def traffic_record():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons, one streaming process sampling every 100 ms
+    while the timed region runs."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -68,29 +69,37 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.samples = []
-        self._stop = threading.Event()
+        self._p = None
         self._t = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([s.strip() for s in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _reader(self):
+        for line in self._p.stdout:
+            line = line.strip()
+            if line:
+                self.samples.append([s.strip() for s in line.split(",")])
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                        "--format=csv,noheader,nounits", "-lms", "100"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._reader, daemon=True)
+            self._t.start()
+            t0 = time.time()
+            while not self.samples and time.time() - t0 < 3.0:
+                time.sleep(0.02)
+        except Exception:
+            self._p = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._p is not None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+            self._t.join(timeout=5)
 
     def summary(self):
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
@@ -297,7 +306,7 @@ def solve_bench(h, D, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -307,7 +316,13 @@ def main():
     ap.add_argument("--nom", type=int, default=24)
     ap.add_argument("--maxrestart", type=int, default=2000)
     ap.add_argument("--tol", type=float, default=5e-11)
+    ap.add_argument("--L", type=int, default=1000,
+                    help="chain length (1000 is the benchmark; smaller sizes are for profiling)")
     args = ap.parse_args()
+    global L_SITES, WORKLOAD
+    if args.L != L_SITES:
+        L_SITES = args.L
+        WORKLOAD = WORKLOAD.replace("L1000", f"L{args.L}")
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local_rank, dist = dist_setup()

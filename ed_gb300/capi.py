@@ -29,6 +29,7 @@ EXPORTS = [
     "qs3g_create", "qs3g_destroy", "qs3g_build_sector", "qs3g_get_sector", "qs3g_hv", "qs3g_hv32",
     "qs3g_connection_table", "qs3g_connection_table_rows", "qs3g_trlan", "qs3g_lanczos", "qs3g_dsf",
     "qs3g_cfrac", "qs3g_last_error", "qs3g_kernel_launches", "qs3g_set_stream", "qs3g_sync",
+    "qs3g_sq_a",
 ]
 
 _lib = None
@@ -238,6 +239,23 @@ class Handle:
                                _ptr(sp), _i(itr_dsf), _d(rfield), _ptr(alpha), _ptr(beta2),
                                _ptr(norm1), _ptr(E0), _ptr(nlev)), self.h)
         return dict(alpha=alpha, beta2=beta2, norm1=norm1, E0=E0, nlev=nlev)
+
+
+def _sq_a(h, psi, spsmsz, qvec, Spos):
+    psi = np.ascontiguousarray(psi, np.complex128)
+    qv = np.ascontiguousarray(np.asarray(qvec, np.float64).reshape(3))
+    sp = np.ascontiguousarray(np.asarray(Spos, np.float64).reshape(-1))
+    Dn = C.c_int64(0)
+    _check(load().qs3g_sq_a(h.h, _ptr(psi), _i(spsmsz), _ptr(qv), _ptr(sp), C.byref(Dn), None, None), h.h)
+    n = int(Dn.value)
+    ls = np.zeros(n, np.int64)
+    fn = np.zeros(n, np.complex128)
+    _check(load().qs3g_sq_a(h.h, _ptr(psi), _i(spsmsz), _ptr(qv), _ptr(sp), C.byref(Dn), _ptr(ls), _ptr(fn)),
+           h.h)
+    return ls, fn
+
+
+Handle.sq_a = lambda self, psi, spsmsz, qvec, Spos: _sq_a(self, psi, spsmsz, qvec, Spos)
 
 
 def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):

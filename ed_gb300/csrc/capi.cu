@@ -302,6 +302,16 @@ int qs3g_dsf(qs3g_handle h, const qs3g_cplx* psi, const double* ene1, const int*
   });
 }
 
+int qs3g_sq_a(qs3g_handle h, const qs3g_cplx* psi, const int* spsmsz, const double* qvec, const double* Spos,
+              int64_t* D_new, int64_t* list_s_new, qs3g_cplx* fn) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(psi && spsmsz && qvec && Spos && D_new, QS3G_EINVAL, "null argument");
+    return sq_a(h->model, s, reinterpret_cast<const double2*>(psi), *spsmsz, qvec, Spos, D_new, list_s_new,
+                reinterpret_cast<double2*>(fn), h->stream);
+  });
+}
+
 int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* alpha, const double* beta2,
                const double* norm1, const double* E0, const double* eta, const int* nomega, const double* omega,
                const int* compat, double* S) {

@@ -41,7 +41,7 @@ struct SqArgs {
   int64_t Dn;
   const uint64_t* conf_new;
   const double* r_new;
-  const uint32_t* dir_gs;
+  const uint2* dir_gs;
   const uint32_t* binomA_gs;  // anchored binomials of the ground-state sector (chains)
   const uint64_t* binom_gs;   // full binomials of the ground-state sector (general lattices)
   const double* r_gs;
@@ -211,6 +211,84 @@ __global__ void k_set_scalar(double2* p, double2 v) { *p = v; }
 
 }  // namespace
 
+// calcu_Sq_a alone for one wave vector: builds the (NOD', k+q) sector in `ns`
+// and writes fn = S^a(q)|psi> (before normalisation) to the device buffer fn.
+void start_vector(const Model& m, const Sector& gs, const double2* d_psi, int spsmsz, const double* qv,
+                  const double* Spos, Sector& ns, DevBuf<double2>& fn, cudaStream_t st) {
+  const int NOD = gs.NOD, NOS = m.NOS;
+  QS3G_REQUIRE(spsmsz >= 1 && spsmsz <= 3, QS3G_EINVAL, "spsmsz must be 1, 2 or 3");
+  QS3G_REQUIRE(!(spsmsz == 1 && NOD <= 1), QS3G_EINVAL, "S+(q,w) needs NOD >= 2");
+  QS3G_REQUIRE(m.chain || spsmsz == 3, QS3G_ENOTSUP, "S+/S- start vectors are implemented for chains");
+  const int NODn = (spsmsz == 1) ? NOD - 1 : (spsmsz == 2 ? NOD + 1 : NOD);
+  double rkn[3] = {gs.rk[0] + qv[0], gs.rk[1] + qv[1], gs.rk[2] + qv[2]};
+  build_sector_rk(m, NODn, rkn, ns, st);
+  const int64_t Dn = ns.D;
+  fn.alloc(std::max<int64_t>(1, Dn));
+  if (Dn == 0) return;
+  std::vector<double2> eks(NOS + 1, make_double2(0.0, 0.0));
+  double2 hsum = make_double2(0.0, 0.0);
+  for (int i = 1; i <= NOS; ++i) {
+    const double d = qv[0] * Spos[3 * (i - 1)] + qv[1] * Spos[3 * (i - 1) + 1] + qv[2] * Spos[3 * (i - 1) + 2];
+    eks[i] = make_double2(std::cos(d), -std::sin(d));
+    hsum.x += eks[i].x;
+    hsum.y += eks[i].y;
+  }
+  DevBuf<double2> d_eks(NOS + 1), d_ph;
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_eks.get(), eks.data(), (NOS + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
+  const double2* ph_new = ns.d_chainph.get();
+  if (!m.chain) {
+    d_ph.alloc(1);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(d_ph.get(), ns.d_explist.get(), sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    ph_new = d_ph.get();
+  }
+  SqArgs a{};
+  a.L = NOS; a.bits = m.bits; a.NOD = NOD; a.NODn = NODn; a.Dn = Dn;
+  a.conf_new = ns.d_conf.get(); a.r_new = ns.d_list_r.get();
+  a.dir_gs = gs.d_dir.get(); a.binomA_gs = gs.d_binomA.get(); a.binom_gs = gs.d_binom.get();
+  a.r_gs = gs.d_list_r.get(); a.psi = d_psi; a.eks = d_eks.get(); a.ph_new = ph_new;
+  a.eks_half_sum = make_double2(0.5 * hsum.x, 0.5 * hsum.y);
+  a.inv_sqrt_nos = 1.0 / std::sqrt((double)NOS);
+  a.fn = fn.get();
+  const unsigned grid = (unsigned)((Dn + 127) / 128);
+  if (spsmsz == 2) {
+    dispatch_nod2(NODn, [&](auto c) {
+      constexpr int V = decltype(c)::value;
+      if constexpr (V >= 2) k_sq_minus_chain<V><<<grid, 128, 0, st>>>(a);
+      else throw Error(QS3G_EINVAL, "S- needs NOD >= 1");
+    });
+    check_launch("k_sq_minus_chain");
+  } else if (spsmsz == 1) {
+    dispatch_nod2(NODn, [&](auto c) {
+      constexpr int V = decltype(c)::value;
+      if constexpr (V + 1 <= 7) k_sq_plus_chain<V><<<grid, 128, 0, st>>>(a);
+      else throw Error(QS3G_ENOTSUP, "S+ with NOD > 7");
+    });
+    check_launch("k_sq_plus_chain");
+  } else {
+    dispatch_nod2(NODn, [&](auto c) {
+      k_sq_z<decltype(c)::value><<<grid, 128, 0, st>>>(a, m.chain ? 1 : 0, NOS);
+    });
+    check_launch("k_sq_z");
+  }
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+int sq_a(const Model& m, const Sector& gs, const double2* h_psi, int spsmsz, const double* qv, const double* Spos,
+         int64_t* Dn_out, int64_t* list_s_new, double2* h_fn, cudaStream_t st) {
+  DevBuf<double2> d_psi(std::max<int64_t>(1, gs.D));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_psi.get(), h_psi, gs.D * sizeof(double2), cudaMemcpyHostToDevice, st));
+  Sector ns;
+  DevBuf<double2> fn;
+  start_vector(m, gs, d_psi.get(), spsmsz, qv, Spos, ns, fn, st);
+  *Dn_out = ns.D;
+  if (ns.D > 0 && list_s_new)
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(list_s_new, ns.d_list_s.get(), ns.D * 8, cudaMemcpyDeviceToHost, st));
+  if (ns.D > 0 && h_fn)
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(h_fn, fn.get(), ns.D * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  return QS3G_OK;
+}
+
 int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int spsmsz, int nq, const double* qvec,
         const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2, double* norm1, double* E0,
         int* nlev, cudaStream_t st) {
@@ -235,10 +313,10 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
   double2* dk = d_ab.get() + 2 * (itr_dsf + 3); // constants
   for (int q = 0; q < nq; ++q) {
     const double* qv = qvec + 3 * (size_t)q;
-    // rk_new = rk + q (get_expectation_values.f90:431-433)
-    double rkn[3] = {gs.rk[0] + qv[0], gs.rk[1] + qv[1], gs.rk[2] + qv[2]};
+    // new sector (N_down', k + q) and fn = S^a(q)|GS> (get_expectation_values.f90:431-491)
     Sector ns;
-    build_sector_rk(m, NODn, rkn, ns, st);
+    DevBuf<double2> f0;
+    start_vector(m, gs, d_psi.get(), spsmsz, qv, Spos, ns, f0, st);
     const int64_t Dn = ns.D;
     E0[q] = ene1 - rfield * sztot;
     for (int k = 0; k < itr_dsf; ++k) {
@@ -246,53 +324,7 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
       beta2[(size_t)q * itr_dsf + k] = 0.0;
     }
     if (Dn == 0) { norm1[q] = 0.0; nlev[q] = 0; continue; }
-    // exp(-i q.R_i) (get_expectation_values.f90:302-304)
-    std::vector<double2> eks(NOS + 1, make_double2(0.0, 0.0));
-    double2 hsum = make_double2(0.0, 0.0);
-    for (int i = 1; i <= NOS; ++i) {
-      const double d = qv[0] * Spos[3 * (i - 1)] + qv[1] * Spos[3 * (i - 1) + 1] + qv[2] * Spos[3 * (i - 1) + 2];
-      eks[i] = make_double2(std::cos(d), -std::sin(d));
-      hsum.x += eks[i].x;
-      hsum.y += eks[i].y;
-    }
-    DevBuf<double2> d_eks(NOS + 1), d_ph;
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(d_eks.get(), eks.data(), (NOS + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
-    const double2* ph_new = ns.d_chainph.get();
-    if (!m.chain) {  // S^z on a general lattice only needs explist_new(0,0,0)
-      d_ph.alloc(1);
-      QS3G_CHECK_CUDA(cudaMemcpyAsync(d_ph.get(), ns.d_explist.get(), sizeof(double2), cudaMemcpyDeviceToDevice, st));
-      ph_new = d_ph.get();
-    }
-    DevBuf<double2> f0(Dn), f1(Dn), f2(Dn);
-    SqArgs a{};
-    a.L = NOS; a.bits = m.bits; a.NOD = NOD; a.NODn = NODn; a.Dn = Dn;
-    a.conf_new = ns.d_conf.get(); a.r_new = ns.d_list_r.get();
-    a.dir_gs = gs.d_dir.get(); a.binomA_gs = gs.d_binomA.get(); a.binom_gs = gs.d_binom.get();
-    a.r_gs = gs.d_list_r.get(); a.psi = d_psi.get(); a.eks = d_eks.get(); a.ph_new = ph_new;
-    a.eks_half_sum = make_double2(0.5 * hsum.x, 0.5 * hsum.y);
-    a.inv_sqrt_nos = 1.0 / std::sqrt((double)NOS);
-    a.fn = f0.get();
-    const unsigned grid = (unsigned)((Dn + 127) / 128);
-    if (spsmsz == 2) {
-      dispatch_nod2(NODn, [&](auto c) {
-        constexpr int V = decltype(c)::value;
-        if constexpr (V >= 2) k_sq_minus_chain<V><<<grid, 128, 0, st>>>(a);
-        else throw Error(QS3G_EINVAL, "S- needs NOD >= 1");
-      });
-      check_launch("k_sq_minus_chain");
-    } else if (spsmsz == 1) {
-      dispatch_nod2(NODn, [&](auto c) {
-        constexpr int V = decltype(c)::value;
-        if constexpr (V + 1 <= 7) k_sq_plus_chain<V><<<grid, 128, 0, st>>>(a);
-        else throw Error(QS3G_ENOTSUP, "S+ with NOD > 7");
-      });
-      check_launch("k_sq_plus_chain");
-    } else {
-      dispatch_nod2(NODn, [&](auto c) {
-        k_sq_z<decltype(c)::value><<<grid, 128, 0, st>>>(a, m.chain ? 1 : 0, NOS);
-      });
-      check_launch("k_sq_z");
-    }
+    DevBuf<double2> f1(Dn), f2(Dn);
     // recursion (get_expectation_values.f90:486-592)
     double2* fn = f0.get();
     double2* fnp1 = f1.get();

@@ -43,7 +43,7 @@ struct HvArgs {
   const uint64_t* conf;
   const double* list_r;
   const float* list_r32;
-  const uint32_t* dir;
+  const uint2* dir;
   const uint32_t* binomA;
   const uint64_t* binom;
   const int* adj_off;
@@ -56,103 +56,92 @@ struct HvArgs {
   const float2* chainph32;
   const double2* explist;
   const int16_t* xyz;
+  const double* diag;      // H(i,i), precomputed at sector build
+  const float* diag32;
+  const double* coefR;     // chains: sJxy_b * list_r for a representative with c self-translations
+  const float* coefR32;    //         [b * (NOD + 1) + c]
+  const double* invR;      // chains: 1 / list_r by self-translation count
+  const float* invR32;
 };
 
 constexpr int kHvThreads = 256;
 
-// ------------------------------------------------------------ chain, complex(8)
+// ------------------------------------------------------------ chain kernels
+// One thread per row.  The row's diagonal is precomputed at sector build
+// (diag[i]); every hop costs two FP64 FMAs: the coefficient
+// sJxy_b * list_r(id) comes from a (bond, self-translation count) table,
+// because a chain representative's norm depends only on that count, which
+// chain_rep_count returns with the representative -- so list_r(id) is never
+// gathered.  The 1/list_r(i) factor is applied once per row.
+template <class V>
+struct Cplx;
+template <>
+struct Cplx<double2> {
+  using R = double;
+  static __device__ __forceinline__ double2 mul(double2 a, double2 b) { return cmul(a, b); }
+};
+template <>
+struct Cplx<float2> {
+  using R = float;
+  static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return cmulf(a, b); }
+};
+
+template <int NOD, bool KZERO, class V>
+__device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
+                                             const typename Cplx<V>::R* __restrict__ diag,
+                                             const typename Cplx<V>::R* __restrict__ coefR,
+                                             const typename Cplx<V>::R* __restrict__ invR, const V* __restrict__ ph,
+                                             int64_t i) {
+  using R = typename Cplx<V>::R;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const V xi = x[i];
+  const R di = __ldg(diag + i);
+  R ax = 0, ay = 0;
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) continue;  // parallel bond: diagonal only
+      int o[NOD], p[NOD], ell, cnt;
+      move_spin<NOD>(n, m, e, o);
+      chain_rep_count<NOD>(o, a.L, a.bits, p, ell, cnt);
+      const int id = dir_lookup32(a.dir, anchored_index32<NOD>(p, a.binomA, a.L));
+      if (id < 0) continue;
+      V xv = x[id];
+      if (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+      const R c = __ldg(coefR + (w >> 16) * (NOD + 1) + cnt);
+      ax = fma(c, xv.x, ax);
+      ay = fma(c, xv.y, ay);
+    }
+  }
+  const R ir = __ldg(invR + chain_self_count<NOD>(n, a.L, a.bits));
+  V out;
+  out.x = fma(di, xi.x, ir * ax);
+  out.y = fma(di, xi.y, ir * ay);
+  y[i] = out;
+}
+
 template <int NOD, bool KZERO>
 __global__ void __launch_bounds__(kHvThreads) k_hv_chain64(HvArgs a, const double2* __restrict__ x,
                                                            double2* __restrict__ y) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
-  int n[NOD];
-  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
-  const double2 xi = x[i];
-  const double ri = __ldg(a.list_r + i);
-  const long long rib = __double_as_longlong(ri);
-  double sdown = 0.0, both = 0.0;
-  double2 accs = make_double2(0.0, 0.0), accd = make_double2(0.0, 0.0);
-#pragma unroll
-  for (int m = 0; m < NOD; ++m) {
-    const int d = n[m];
-    sdown += __ldg(a.Sz_site + d);
-    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
-    for (int t = e0; t < e1; ++t) {
-      const uint32_t w = __ldg(a.adj + t);
-      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
-      bool edown = false;
-#pragma unroll
-      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
-      if (edown) { both += __ldg(a.sJz + b); continue; }
-      int o[NOD], p[NOD], ell;
-      move_spin<NOD>(n, m, e, o);
-      chain_rep<NOD>(o, a.L, a.bits, p, ell);
-      const int64_t id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
-      if (id < 0) continue;
-      double2 xv = x[id];
-      const double rv = __ldg(a.list_r + id);
-      const double cj = __ldg(a.sJxy + b);
-      if (!KZERO) xv = cmul(__ldg(a.chainph + ell), xv);
-      if (__double_as_longlong(rv) == rib) {
-        accs.x = fma(cj, xv.x, accs.x);
-        accs.y = fma(cj, xv.y, accs.y);
-      } else {
-        const double cw = cj * rv;
-        accd.x = fma(cw, xv.x, accd.x);
-        accd.y = fma(cw, xv.y, accd.y);
-      }
-    }
-  }
-  const double diag = fma(-2.0, sdown - both, a.Sz_all);
-  double2 out = make_double2(fma(diag, xi.x, accs.x), fma(diag, xi.y, accs.y));
-  if (accd.x != 0.0 || accd.y != 0.0) {
-    const double inv = 1.0 / ri;
-    out.x = fma(inv, accd.x, out.x);
-    out.y = fma(inv, accd.y, out.y);
-  }
-  y[i] = out;
+  hv_chain_row<NOD, KZERO, double2>(a, x, y, a.diag, a.coefR, a.invR, a.chainph, i);
 }
 
-// ------------------------------------------------------------ chain, complex(4)
 template <int NOD, bool KZERO>
 __global__ void __launch_bounds__(kHvThreads) k_hv_chain32(HvArgs a, const float2* __restrict__ x,
                                                            float2* __restrict__ y) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
-  int n[NOD];
-  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
-  const float2 xi = x[i];
-  const float ri = __ldg(a.list_r32 + i);
-  float sdown = 0.f, both = 0.f;
-  float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-  for (int m = 0; m < NOD; ++m) {
-    const int d = n[m];
-    sdown += (float)__ldg(a.Sz_site + d);
-    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
-    for (int t = e0; t < e1; ++t) {
-      const uint32_t w = __ldg(a.adj + t);
-      const int e = (int)(w & 0xffffu), b = (int)(w >> 16);
-      bool edown = false;
-#pragma unroll
-      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
-      if (edown) { both += (float)__ldg(a.sJz + b); continue; }
-      int o[NOD], p[NOD], ell;
-      move_spin<NOD>(n, m, e, o);
-      chain_rep<NOD>(o, a.L, a.bits, p, ell);
-      const int64_t id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
-      if (id < 0) continue;
-      float2 xv = x[id];
-      const float cw = (float)__ldg(a.sJxy + b) * __ldg(a.list_r32 + id);
-      if (!KZERO) xv = cmulf(__ldg(a.chainph32 + ell), xv);
-      acc.x = fmaf(cw, xv.x, acc.x);
-      acc.y = fmaf(cw, xv.y, acc.y);
-    }
-  }
-  const float diag = fmaf(-2.f, sdown - both, (float)a.Sz_all);
-  const float inv = 1.0f / ri;
-  y[i] = make_float2(fmaf(diag, xi.x, inv * acc.x), fmaf(diag, xi.y, inv * acc.y));
+  hv_chain_row<NOD, KZERO, float2>(a, x, y, a.diag32, a.coefR32, a.invR32, a.chainph32, i);
 }
 
 // ------------------------------------------------------------ general lattice helpers
@@ -411,10 +400,50 @@ HvArgs make_args(const Model& m, const Sector& s) {
   a.sJxy = m.d_sJxy.get(); a.sJz = m.d_sJz.get(); a.Sz_site = m.d_Sz_site.get(); a.Sz_all = m.Sz_all;
   a.chainph = s.d_chainph.get(); a.chainph32 = s.d_chainph32.get(); a.explist = s.d_explist.get();
   a.xyz = m.d_site_xyz.get();
+  a.diag = s.d_diag.get(); a.diag32 = s.d_diag32.get();
+  a.coefR = s.d_coefR.get(); a.coefR32 = s.d_coefR32.get();
+  a.invR = s.d_invR.get(); a.invR32 = s.d_invR32.get();
   return a;
 }
 
+// Diagonal of H per row: sum_b sJz_b * (+1 parallel / -1 antiparallel)
+//   = Sz_all - 2 * (sum_{d down} Sz_site[d] - sum over both-down bond ends of sJz_b)
+// (the `f1 .neqv. f2` branches of ham2vec_v3.f90:57-67).
+template <int NOD>
+__global__ void k_diag(HvArgs a, double* diag, float* diag32) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(a.conf[i], a.bits, n);
+  double sdown = 0.0, both = 0.0;
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    sdown += a.Sz_site[d];
+    for (int t = a.adj_off[d]; t < a.adj_off[d + 1]; ++t) {
+      const uint32_t w = a.adj[t];
+      const int e = (int)(w & 0xffffu);
+      bool edown = false;
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) both += a.sJz[w >> 16];
+    }
+  }
+  const double dg = a.Sz_all - 2.0 * (sdown - both);
+  diag[i] = dg;
+  diag32[i] = (float)dg;
+}
+
 }  // namespace
+
+void compute_diag(const Model& m, Sector& s, cudaStream_t st) {
+  s.d_diag.alloc(std::max<int64_t>(1, s.D));
+  s.d_diag32.alloc(std::max<int64_t>(1, s.D));
+  if (s.D == 0) return;
+  HvArgs a = make_args(m, s);
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_diag<decltype(c)::value><<<(unsigned)((s.D + 255) / 256), 256, 0, st>>>(a, s.d_diag.get(), s.d_diag32.get());
+  });
+  check_launch("k_diag");
+}
 
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
   if (s.D == 0) return;

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kRedThreads) k_nrm_part(const T* __restrict__ 
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// out = sum of np partials (mode 0: complex; 1: sqrt(real) into .x; 2: real)
+// out = sum of np partials (mode 0: complex; 1: (sqrt(real), real); 2: real)
 __global__ void __launch_bounds__(kRedThreads) k_red_final(const double2* part, int np, double2* out, int mode) {
   __shared__ double2 sh[kRedThreads];
   double2 acc = make_double2(0.0, 0.0);
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kRedThreads) k_red_final(const double2* part, 
   }
   const double2 s = block_sum2(acc, sh);
   if (threadIdx.x == 0) {
-    if (mode == 1) *out = make_double2(sqrt(s.x), 0.0);
+    if (mode == 1) *out = make_double2(sqrt(s.x), s.x);
     else if (mode == 2) *out = make_double2(s.x, 0.0);
     else *out = s;
   }

@@ -59,8 +59,16 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
         const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2, double* norm1, double* E0,
         int* nlev, cudaStream_t st);
 
+// calcu_Sq_a alone for one wave vector: D' of the new sector, its list_s and
+// fn = S^a(q)|psi> before normalisation (host arrays may be null).
+int sq_a(const Model& m, const Sector& gs, const double2* h_psi, int spsmsz, const double* qv, const double* Spos,
+         int64_t* Dn_out, int64_t* list_s_new, double2* h_fn, cudaStream_t st);
+
 // Sector build for an arbitrary wave vector rk (DSF sectors use rk + q).
 void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cudaStream_t st);
+
+// H(i,i) for every row of the sector (called by the sector build).
+void compute_diag(const Model& m, Sector& s, cudaStream_t st);
 
 int64_t connection_table_rows(const Model& m, const Sector& s, int64_t row0, int64_t row1, int64_t* row,
                               int64_t* col, int* ell, int* bond, int64_t cap, cudaStream_t st);

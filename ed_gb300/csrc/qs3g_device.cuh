@@ -48,32 +48,18 @@ __device__ __forceinline__ void move_spin(const int (&n)[NOD], int m, int e, int
 }
 
 // Directory lookup: candidate index c -> 0-based row, or -1 if c is not a
-// row of the sector.  Blocks are 8 x 32-bit words: word 0 = rows before the
-// block, words 1..7 = presence bits of 224 consecutive candidates.
-__device__ __forceinline__ int64_t dir_lookup(const uint32_t* __restrict__ dir, uint64_t c) {
-  const uint64_t blk = c / 224u;
-  const unsigned bit = (unsigned)(c - blk * 224u);
-  const uint4* bp = reinterpret_cast<const uint4*>(dir) + 2 * blk;
-  const uint4 a = __ldg(bp);
-  const uint4 b = __ldg(bp + 1);
-  const unsigned wi = bit >> 5, bi = bit & 31u;
-  const unsigned w0 = a.y, w1 = a.z, w2 = a.w, w3 = b.x, w4 = b.y, w5 = b.z, w6 = b.w;
-  unsigned word = w0;
-  word = (wi == 1) ? w1 : word;
-  word = (wi == 2) ? w2 : word;
-  word = (wi == 3) ? w3 : word;
-  word = (wi == 4) ? w4 : word;
-  word = (wi == 5) ? w5 : word;
-  word = (wi == 6) ? w6 : word;
-  if (!((word >> bi) & 1u)) return -1;
-  unsigned cnt = __popc(word & ((1u << bi) - 1u));
-  cnt += (wi > 0) ? __popc(w0) : 0u;
-  cnt += (wi > 1) ? __popc(w1) : 0u;
-  cnt += (wi > 2) ? __popc(w2) : 0u;
-  cnt += (wi > 3) ? __popc(w3) : 0u;
-  cnt += (wi > 4) ? __popc(w4) : 0u;
-  cnt += (wi > 5) ? __popc(w5) : 0u;
-  return (int64_t)a.x + (int64_t)cnt;
+// row of the sector.  One 8-byte entry per 32 consecutive candidates:
+// .x = rows before the entry, .y = presence bits, so a lookup is one load,
+// a mask and a popcount.
+__device__ __forceinline__ int dir_lookup(const uint2* __restrict__ dir, uint64_t c) {
+  const uint2 w = __ldg(dir + (c >> 5));
+  const unsigned b = (unsigned)c & 31u;
+  return ((w.y >> b) & 1u) ? (int)(w.x + __popc(w.y & ((1u << b) - 1u))) : -1;
+}
+__device__ __forceinline__ int dir_lookup32(const uint2* __restrict__ dir, uint32_t c) {
+  const uint2 w = __ldg(dir + (c >> 5));
+  const unsigned b = c & 31u;
+  return ((w.y >> b) & 1u) ? (int)(w.x + __popc(w.y & ((1u << b) - 1u))) : -1;
 }
 
 // Chain representative (LY = LZ = 1).  Among the L translations of a
@@ -95,21 +81,43 @@ __device__ __forceinline__ void chain_rep(const int (&n)[NOD], int L, int bits, 
 #pragma unroll
   for (int m = 0; m < NOD - 1; ++m) g[m] = n[m + 1] - n[m];
   g[NOD - 1] = n[0] + L - n[NOD - 1];
-  uint64_t best = 0, key0 = 0;
-  int bm = 0;
+  // The first key component of rotation m is g[m-1]: when the largest gap is
+  // unique, its successor wins without comparing whole keys.
+  int gmax = g[0], am = 0, ties = 1;
 #pragma unroll
-  for (int m = 0; m < NOD; ++m) {
-    uint64_t key = 0;
+  for (int m = 1; m < NOD; ++m) {
+    ties = (g[m] == gmax) ? ties + 1 : ((g[m] > gmax) ? 1 : ties);
+    am = (g[m] > gmax) ? m : am;
+    gmax = max(gmax, g[m]);
+  }
+  int bm;
+  bool orig;
+  if (ties == 1) {
+    bm = (am + 1 == NOD) ? 0 : am + 1;
+    orig = (bm == 0) && (n[0] == 1);
+  } else {
+    uint64_t best = 0, key0 = 0;
+    bm = 0;
 #pragma unroll
-    for (int t = 1; t <= NOD; ++t) key = (key << bits) | (uint64_t)g[(m - t + 2 * NOD) % NOD];
-    if (m == 0) key0 = key;
-    if (key >= best) { best = key; bm = m; }
+    for (int m = 0; m < NOD; ++m) {
+      uint64_t key = 0;
+#pragma unroll
+      for (int t = 1; t <= NOD; ++t) key = (key << bits) | (uint64_t)g[(m - t + 2 * NOD) % NOD];
+      if (m == 0) key0 = key;
+      if (key >= best) { best = key; bm = m; }
+    }
+    orig = (n[0] == 1) && (key0 == best);
+  }
+  if (orig) {  // already the representative: ell = 0
+    ell = 0;
+#pragma unroll
+    for (int j = 0; j < NOD; ++j) p[j] = n[j];
+    return;
   }
   int nb = n[0];
 #pragma unroll
   for (int m = 1; m < NOD; ++m) nb = (bm == m) ? n[m] : nb;
-  const bool orig = (n[0] == 1) && (key0 == best);
-  ell = orig ? 0 : (L - nb + 1);
+  ell = L - nb + 1;
   // positions of the winning rotation
   p[0] = 1;
 #pragma unroll
@@ -119,6 +127,111 @@ __device__ __forceinline__ void chain_rep(const int (&n)[NOD], int L, int bits, 
     for (int m = 1; m < NOD; ++m) gj = (((bm + j - 1) % NOD) == m) ? g[m] : gj;
     p[j] = p[j - 1] + gj;
   }
+}
+
+// chain_rep plus the number of self-translations of the representative
+// (translations i in 1..L with T^i rep = rep): 1 when the largest gap is
+// unique, else the number of rotations whose key equals the winning key.
+// The norm of a chain representative depends only on this count.
+template <int NOD>
+__device__ __forceinline__ void chain_rep_count(const int (&n)[NOD], int L, int bits, int (&p)[NOD], int& ell,
+                                                int& cnt) {
+  int g[NOD];
+#pragma unroll
+  for (int m = 0; m < NOD - 1; ++m) g[m] = n[m + 1] - n[m];
+  g[NOD - 1] = n[0] + L - n[NOD - 1];
+  int gmax = g[0], am = 0, ties = 1;
+#pragma unroll
+  for (int m = 1; m < NOD; ++m) {
+    ties = (g[m] == gmax) ? ties + 1 : ((g[m] > gmax) ? 1 : ties);
+    am = (g[m] > gmax) ? m : am;
+    gmax = max(gmax, g[m]);
+  }
+  int bm;
+  bool orig;
+  if (ties == 1) {
+    bm = (am + 1 == NOD) ? 0 : am + 1;
+    orig = (bm == 0) && (n[0] == 1);
+    cnt = 1;
+  } else {
+    uint64_t best = 0, key0 = 0;
+    uint64_t key[NOD];
+    bm = 0;
+#pragma unroll
+    for (int m = 0; m < NOD; ++m) {
+      uint64_t k = 0;
+#pragma unroll
+      for (int t = 1; t <= NOD; ++t) k = (k << bits) | (uint64_t)g[(m - t + 2 * NOD) % NOD];
+      key[m] = k;
+      if (m == 0) key0 = k;
+      if (k >= best) { best = k; bm = m; }
+    }
+    cnt = 0;
+#pragma unroll
+    for (int m = 0; m < NOD; ++m) cnt += (key[m] == best) ? 1 : 0;
+    orig = (n[0] == 1) && (key0 == best);
+  }
+  if (orig) {
+    ell = 0;
+#pragma unroll
+    for (int j = 0; j < NOD; ++j) p[j] = n[j];
+    return;
+  }
+  int nb = n[0];
+#pragma unroll
+  for (int m = 1; m < NOD; ++m) nb = (bm == m) ? n[m] : nb;
+  ell = L - nb + 1;
+  p[0] = 1;
+#pragma unroll
+  for (int j = 1; j < NOD; ++j) {
+    int gj = g[0];
+#pragma unroll
+    for (int m = 1; m < NOD; ++m) gj = (((bm + j - 1) % NOD) == m) ? g[m] : gj;
+    p[j] = p[j - 1] + gj;
+  }
+}
+
+// Number of self-translations of a chain representative p (p[0] = 1, key_0 maximal).
+template <int NOD>
+__device__ __forceinline__ int chain_self_count(const int (&p)[NOD], int L, int bits) {
+  int g[NOD];
+#pragma unroll
+  for (int m = 0; m < NOD - 1; ++m) g[m] = p[m + 1] - p[m];
+  g[NOD - 1] = p[0] + L - p[NOD - 1];
+  int gmax = g[0], ties = 1;
+#pragma unroll
+  for (int m = 1; m < NOD; ++m) {
+    ties = (g[m] == gmax) ? ties + 1 : ((g[m] > gmax) ? 1 : ties);
+    gmax = max(gmax, g[m]);
+  }
+  if (ties == 1) return 1;
+  uint64_t key0 = 0;
+#pragma unroll
+  for (int t = 1; t <= NOD; ++t) key0 = (key0 << bits) | (uint64_t)g[(0 - t + 2 * NOD) % NOD];
+  int cnt = 1;
+#pragma unroll
+  for (int m = 1; m < NOD; ++m) {
+    uint64_t k = 0;
+#pragma unroll
+    for (int t = 1; t <= NOD; ++t) k = (k << bits) | (uint64_t)g[(m - t + 2 * NOD) % NOD];
+    cnt += (k == key0) ? 1 : 0;
+  }
+  return cnt;
+}
+
+// Anchored candidate index with 32-bit arithmetic: C(x,1) = x and
+// C(x,2) = x(x-1)/2 in registers, higher binomials from the table.
+template <int NOD>
+__device__ __forceinline__ uint32_t anchored_index32(const int (&p)[NOD], const uint32_t* __restrict__ binomA, int L) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int j = 1; j < NOD; ++j) {
+    const uint32_t x = (uint32_t)(p[j] - 2);
+    if (j == 1) c += x;
+    else if (j == 2) c += (x * (x - 1u)) >> 1;
+    else c += __ldg(binomA + (size_t)(j - 1) * (L - 1) + x);
+  }
+  return c;
 }
 
 // Anchored candidate index of a configuration with p[0] = 1:

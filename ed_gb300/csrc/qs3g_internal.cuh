@@ -74,8 +74,7 @@ struct DevBuf {
 
 // ---------------------------------------------------------------- limits
 constexpr int kMaxNOD = 8;          // template instantiations of the row kernels
-constexpr int kDirBits = 224;       // candidates per 32-byte directory block
-constexpr int kDirWords = 8;        // base (1 word) + 7 bit words
+constexpr int kDirBlock = 256;      // candidates per build thread (8 directory entries)
 
 // ---------------------------------------------------------------- model
 // Lattice + bonds as read by read_ip (input_param.f90:58-117).
@@ -107,17 +106,22 @@ struct Sector {
   bool kzero = false;               // every phase equals exp(0) = 1 exactly
   uint64_t nspace = 0;              // candidates in the directory space
   int64_t D = 0;
-  uint64_t nblocks = 0;             // directory blocks
+  uint64_t nblocks = 0;             // build blocks of 256 candidates
+  uint64_t nwords = 0;              // directory entries (32 candidates each)
   DevBuf<int64_t> d_list_s;         // colex ranks (1-based), ascending
   DevBuf<double> d_list_r;          // sqrt(norm^2)
   DevBuf<float> d_list_r32;         // float copy for the complex(4) kernels
   DevBuf<uint64_t> d_conf;          // packed sorted down-spin sites
-  DevBuf<uint32_t> d_dir;           // nblocks x 8 words: base row, 224 presence bits
+  DevBuf<uint2> d_dir;              // per 32 candidates: (rows before, presence bits)
   DevBuf<double2> d_explist;        // explist(0:LX,0:LY,0:LZ), Fortran order
   DevBuf<double2> d_chainph;        // chain: explist(i,1,1) for i = 1..LX, [0] = explist(0,0,0)
   DevBuf<float2> d_chainph32;
   DevBuf<uint64_t> d_binom;         // C(n,k) for n in [0,NOS], k in [0,NOD+1]: [k*(NOS+1)+n]
   DevBuf<uint32_t> d_binomA;        // anchored: C(x,k) for x in [0,NOS-2], k in [1,NOD-1] (u32)
+  DevBuf<double> d_diag;            // H(i,i)
+  DevBuf<float> d_diag32;
+  DevBuf<double> d_coefR, d_invR;   // chains: sJxy_b * R[c] and 1/R[c] by self-translation count c
+  DevBuf<float> d_coefR32, d_invR32;
 };
 
 // Host-side explist (input_param.f90:87-89) and checkstate phases

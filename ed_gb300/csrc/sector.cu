@@ -4,7 +4,7 @@
 // 225-292).  The reference tests every one of the C(NOS, NOD) ranks with a
 // full translation scan, stores the survivors with a critical section and
 // quick-sorts them.  Here candidates are enumerated in colex (= rank) order
-// by one thread per directory block of 224 candidates, the survivors are
+// by one thread per block of 256 candidates, the survivors are
 // marked in a presence bitmap, one exclusive scan turns the bitmap into row
 // numbers, and a second pass writes the rows in rank order -- already sorted.
 // The bitmap plus its block bases (the "directory") is kept as the O(1)
@@ -64,6 +64,18 @@ namespace {
 
 constexpr int kThreads = 128;
 
+// Store the 8 presence words of 256-candidate block b as directory entries
+// with their prefix counts inside the block; returns the block's count.
+__device__ __forceinline__ uint32_t write_words(uint2* dirw, uint64_t nwords, uint64_t b, const uint32_t (&w)[8]) {
+  uint32_t pre = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (b * 8 + k < nwords) dirw[b * 8 + k] = make_uint2(pre, w[k]);
+    pre += __popc(w[k]);
+  }
+  return pre;
+}
+
 // ------------------------------------------------------------ chain (anchored space)
 struct ChainBuildArgs {
   int L, NOD, bits;
@@ -72,7 +84,8 @@ struct ChainBuildArgs {
   const uint64_t* binom;    // C(n, k), k in [0, NOD+1]
   const int* keep;          // keep[count] for count in [1, NOD]
   const double* r_by_count; // list_r value for a representative with `count` self-translations
-  uint32_t* dir;
+  uint2* dirw;              // one entry per 32 candidates: (rows before, presence bits)
+  uint64_t nwords;
   uint32_t* blkcount;
   int64_t* list_s;
   double* list_r;
@@ -151,42 +164,35 @@ template <int NOD>
 __global__ void __launch_bounds__(kThreads) k_chain_mark(ChainBuildArgs a) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.nblocks) return;
-  const uint64_t c0 = b * 224u;
+  const uint64_t c0 = b * 256u;
   int q[NOD];
   anchored_unrank<NOD>(c0, a, q);
-  uint32_t words[7] = {0, 0, 0, 0, 0, 0, 0};
-  uint32_t cnt = 0;
-  const int kmax = (int)((a.nspace - c0) < 224u ? (a.nspace - c0) : 224u);
+  uint32_t words[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int kmax = (int)((a.nspace - c0) < 256u ? (a.nspace - c0) : 256u);
   for (int k = 0; k < kmax; ++k) {
     int p[NOD];
     p[0] = 1;
 #pragma unroll
     for (int j = 1; j < NOD; ++j) p[j] = q[j] + 2;
     const int sc = chain_selfcount<NOD>(p, a.L, a.bits);
-    if (sc > 0 && a.keep[sc]) {
-      words[k >> 5] |= 1u << (k & 31);
-      ++cnt;
-    }
+    if (sc > 0 && a.keep[sc]) words[k >> 5] |= 1u << (k & 31);
     anchored_next<NOD>(q);
   }
-  uint32_t* d = a.dir + b * 8;
-#pragma unroll
-  for (int w = 0; w < 7; ++w) d[1 + w] = words[w];
-  a.blkcount[b] = cnt;
+  a.blkcount[b] = write_words(a.dirw, a.nwords, b, words);
 }
 
 template <int NOD>
 __global__ void __launch_bounds__(kThreads) k_chain_emit(ChainBuildArgs a) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.nblocks) return;
-  const uint64_t c0 = b * 224u;
-  const uint32_t* d = a.dir + b * 8;
-  uint32_t row = d[0];
+  const uint64_t c0 = b * 256u;
+  const uint2* d = a.dirw + b * 8;
+  uint32_t row = d[0].x;
   int q[NOD];
   anchored_unrank<NOD>(c0, a, q);
-  const int kmax = (int)((a.nspace - c0) < 224u ? (a.nspace - c0) : 224u);
+  const int kmax = (int)((a.nspace - c0) < 256u ? (a.nspace - c0) : 256u);
   for (int k = 0; k < kmax; ++k) {
-    if ((d[1 + (k >> 5)] >> (k & 31)) & 1u) {
+    if ((d[k >> 5].y >> (k & 31)) & 1u) {
       int p[NOD];
       p[0] = 1;
 #pragma unroll
@@ -214,7 +220,8 @@ struct GenBuildArgs {
   const int16_t* xyz;        // (x,y,z,pad) per site, index 1..NOS
   const double2* phase;      // checkstate phase per translation (loop order)
   double NOSd;
-  uint32_t* dir;
+  uint2* dirw;
+  uint64_t nwords;
   uint32_t* blkcount;
   int64_t* list_s;
   uint64_t* conf;
@@ -300,12 +307,11 @@ template <int NOD>
 __global__ void __launch_bounds__(kThreads) k_gen_mark(GenBuildArgs a) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.nblocks) return;
-  const uint64_t c0 = b * 224u;
+  const uint64_t c0 = b * 256u;
   int v[NOD];
   full_unrank<NOD>(c0, a, v);
-  uint32_t words[7] = {0, 0, 0, 0, 0, 0, 0};
-  uint32_t cnt = 0;
-  const int kmax = (int)((a.nspace - c0) < 224u ? (a.nspace - c0) : 224u);
+  uint32_t words[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int kmax = (int)((a.nspace - c0) < 256u ? (a.nspace - c0) : 256u);
   for (int k = 0; k < kmax; ++k) {
     int n[NOD];
 #pragma unroll
@@ -314,31 +320,25 @@ __global__ void __launch_bounds__(kThreads) k_gen_mark(GenBuildArgs a) {
     double2 coef;
     if (general_check<NOD>(n, a, count, coef)) {
       const double ro = (coef.x * coef.x + coef.y * coef.y) * a.NOSd / (double)count;
-      if (ro > 1.0e-15) {
-        words[k >> 5] |= 1u << (k & 31);
-        ++cnt;
-      }
+      if (ro > 1.0e-15) words[k >> 5] |= 1u << (k & 31);
     }
     full_next<NOD>(v);
   }
-  uint32_t* d = a.dir + b * 8;
-#pragma unroll
-  for (int w = 0; w < 7; ++w) d[1 + w] = words[w];
-  a.blkcount[b] = cnt;
+  a.blkcount[b] = write_words(a.dirw, a.nwords, b, words);
 }
 
 template <int NOD>
 __global__ void __launch_bounds__(kThreads) k_gen_emit(GenBuildArgs a) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.nblocks) return;
-  const uint64_t c0 = b * 224u;
-  const uint32_t* d = a.dir + b * 8;
-  uint32_t row = d[0];
+  const uint64_t c0 = b * 256u;
+  const uint2* d = a.dirw + b * 8;
+  uint32_t row = d[0].x;
   int v[NOD];
   full_unrank<NOD>(c0, a, v);
-  const int kmax = (int)((a.nspace - c0) < 224u ? (a.nspace - c0) : 224u);
+  const int kmax = (int)((a.nspace - c0) < 256u ? (a.nspace - c0) : 256u);
   for (int k = 0; k < kmax; ++k) {
-    if ((d[1 + (k >> 5)] >> (k & 31)) & 1u) {
+    if ((d[k >> 5].y >> (k & 31)) & 1u) {
       int n[NOD];
 #pragma unroll
       for (int j = 0; j < NOD; ++j) n[j] = v[j] + 1;
@@ -356,9 +356,9 @@ __global__ void __launch_bounds__(kThreads) k_gen_emit(GenBuildArgs a) {
 }
 
 // ------------------------------------------------------------ scan of block counts
-__global__ void k_scan_blocks(const uint32_t* in, uint64_t n, uint64_t* partial, uint32_t* out_base,
-                              int pass) {
-  // pass 0: per CTA sums of 1024-element chunks; pass 1: write exclusive bases
+// Exclusive scan of per-block counts: pass 0 sums 1024-block chunks, the host
+// scans the chunk sums, pass 1 writes every block's base.
+__global__ void k_scan_blocks(const uint32_t* in, uint64_t n, uint64_t* partial, uint64_t* out_base, int pass) {
   __shared__ uint64_t sh[1024];
   const uint64_t base = (uint64_t)blockIdx.x * 1024u;
   const uint64_t i = base + threadIdx.x;
@@ -374,8 +374,14 @@ __global__ void k_scan_blocks(const uint32_t* in, uint64_t n, uint64_t* partial,
   if (pass == 0) {
     if (threadIdx.x == 1023) partial[blockIdx.x] = sh[1023];
   } else {
-    if (i < n) out_base[i * 8] = (uint32_t)(partial[blockIdx.x] + sh[threadIdx.x] - v);
+    if (i < n) out_base[i] = partial[blockIdx.x] + sh[threadIdx.x] - v;
   }
+}
+
+// dirw[w].x += base of its 256-candidate block
+__global__ void k_dir_fix(uint2* dirw, uint64_t nwords, const uint64_t* base) {
+  const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < nwords) dirw[w].x += (uint32_t)base[w >> 3];
 }
 
 template <class F>
@@ -393,11 +399,11 @@ void dispatch_nod(int NOD, F&& f) {
   }
 }
 
-// Exclusive scan of nblocks block counts into dir[b*8]; returns the total.
-uint64_t scan_directory(uint32_t* blkcount, uint64_t nblocks, uint32_t* dir, cudaStream_t st) {
+// Exclusive scan of the block counts, folded into the directory; returns the total.
+uint64_t scan_directory(uint32_t* blkcount, uint64_t nblocks, uint2* dirw, uint64_t nwords, cudaStream_t st) {
   const uint64_t nchunks = (nblocks + 1023) / 1024;
-  DevBuf<uint64_t> d_partial(nchunks);
-  k_scan_blocks<<<(unsigned)nchunks, 1024, 0, st>>>(blkcount, nblocks, d_partial.get(), dir, 0);
+  DevBuf<uint64_t> d_partial(nchunks), d_base(nblocks);
+  k_scan_blocks<<<(unsigned)nchunks, 1024, 0, st>>>(blkcount, nblocks, d_partial.get(), d_base.get(), 0);
   check_launch("k_scan_blocks");
   std::vector<uint64_t> h(nchunks);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(h.data(), d_partial.get(), nchunks * 8, cudaMemcpyDeviceToHost, st));
@@ -405,8 +411,10 @@ uint64_t scan_directory(uint32_t* blkcount, uint64_t nblocks, uint32_t* dir, cud
   uint64_t run = 0;
   for (uint64_t c = 0; c < nchunks; ++c) { uint64_t t = h[c]; h[c] = run; run += t; }
   QS3G_CHECK_CUDA(cudaMemcpyAsync(d_partial.get(), h.data(), nchunks * 8, cudaMemcpyHostToDevice, st));
-  k_scan_blocks<<<(unsigned)nchunks, 1024, 0, st>>>(blkcount, nblocks, d_partial.get(), dir, 1);
+  k_scan_blocks<<<(unsigned)nchunks, 1024, 0, st>>>(blkcount, nblocks, d_partial.get(), d_base.get(), 1);
   check_launch("k_scan_blocks");
+  k_dir_fix<<<(unsigned)((nwords + 255) / 256), 256, 0, st>>>(dirw, nwords, d_base.get());
+  check_launch("k_dir_fix");
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
   return run;
 }
@@ -492,21 +500,22 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
     DevBuf<double> d_rbc(NOD + 1);
     QS3G_CHECK_CUDA(cudaMemcpyAsync(d_keep.get(), keep.data(), (NOD + 1) * 4, cudaMemcpyHostToDevice, st));
     QS3G_CHECK_CUDA(cudaMemcpyAsync(d_rbc.get(), rbc.data(), (NOD + 1) * 8, cudaMemcpyHostToDevice, st));
-    s.nblocks = (s.nspace + 223) / 224;
-    s.d_dir.alloc(s.nblocks * 8);
+    s.nblocks = (s.nspace + 255) / 256;
+    s.nwords = (s.nspace + 31) / 32;
+    s.d_dir.alloc(s.nwords);
     DevBuf<uint32_t> d_cnt(s.nblocks);
     ChainBuildArgs a{};
     a.L = L; a.NOD = NOD; a.bits = m.bits; a.nspace = s.nspace; a.nblocks = s.nblocks;
     a.binomA = s.d_binomA.get(); a.binom = s.d_binom.get();
     a.keep = d_keep.get(); a.r_by_count = d_rbc.get();
-    a.dir = s.d_dir.get(); a.blkcount = d_cnt.get();
+    a.dirw = s.d_dir.get(); a.nwords = s.nwords; a.blkcount = d_cnt.get();
     const unsigned grid = (unsigned)((s.nblocks + kThreads - 1) / kThreads);
     dispatch_nod(NOD, [&](auto c) {
       k_chain_mark<decltype(c)::value><<<grid, kThreads, 0, st>>>(a);
     });
     check_launch("k_chain_mark");
-    const uint64_t D = scan_directory(d_cnt.get(), s.nblocks, s.d_dir.get(), st);
-    QS3G_REQUIRE(D < (1ull << 32), QS3G_ERANGE, "sector dimension exceeds 2^32");
+    const uint64_t D = scan_directory(d_cnt.get(), s.nblocks, s.d_dir.get(), s.nwords, st);
+    QS3G_REQUIRE(D < (1ull << 31), QS3G_ERANGE, "sector dimension exceeds 2^31");
     s.D = (int64_t)D;
     s.d_list_s.alloc(D); s.d_list_r.alloc(D); s.d_list_r32.alloc(D); s.d_conf.alloc(D);
     a.list_s = s.d_list_s.get(); a.list_r = s.d_list_r.get(); a.list_r32 = s.d_list_r32.get();
@@ -517,6 +526,21 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
       });
       check_launch("k_chain_emit");
     }
+    // H*v coefficient tables: sJxy_b * R[c] and 1/R[c] by self-translation count
+    std::vector<double> cr((size_t)std::max(1, m.NOxxz) * (NOD + 1), 0.0), ir(NOD + 1, 0.0);
+    std::vector<float> cr32(cr.size()), ir32(NOD + 1);
+    for (int b = 0; b < m.NOxxz; ++b)
+      for (int c = 0; c <= NOD; ++c) cr[(size_t)b * (NOD + 1) + c] = m.sJxy[b] * rbc[c];
+    for (int c = 0; c <= NOD; ++c) ir[c] = rbc[c] > 0.0 ? 1.0 / rbc[c] : 0.0;
+    for (size_t k = 0; k < cr.size(); ++k) cr32[k] = (float)cr[k];
+    for (int c = 0; c <= NOD; ++c) ir32[c] = (float)ir[c];
+    s.d_coefR.alloc(cr.size()); s.d_coefR32.alloc(cr.size());
+    s.d_invR.alloc(NOD + 1); s.d_invR32.alloc(NOD + 1);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_coefR.get(), cr.data(), cr.size() * 8, cudaMemcpyHostToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_coefR32.get(), cr32.data(), cr32.size() * 4, cudaMemcpyHostToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_invR.get(), ir.data(), (NOD + 1) * 8, cudaMemcpyHostToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_invR32.get(), ir32.data(), (NOD + 1) * 4, cudaMemcpyHostToDevice, st));
+    compute_diag(m, s, st);
     QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
     return;
   }
@@ -542,22 +566,23 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
   }
   DevBuf<double2> d_phase(NT);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(d_phase.get(), phase.data(), NT * sizeof(double2), cudaMemcpyHostToDevice, st));
-  s.nblocks = (s.nspace + 223) / 224;
-  s.d_dir.alloc(s.nblocks * 8);
+  s.nblocks = (s.nspace + 255) / 256;
+  s.nwords = (s.nspace + 31) / 32;
+  s.d_dir.alloc(s.nwords);
   DevBuf<uint32_t> d_cnt(s.nblocks);
   GenBuildArgs a{};
   a.NOS = m.NOS; a.NOD = NOD; a.bits = m.bits; a.LX = m.LX; a.LY = m.LY; a.LZ = m.LZ; a.NT = NT;
   a.nspace = s.nspace; a.nblocks = s.nblocks; a.binom = s.d_binom.get();
   a.xyz = m.d_site_xyz.get(); a.phase = d_phase.get(); a.NOSd = (double)m.NOS;
-  a.dir = s.d_dir.get(); a.blkcount = d_cnt.get();
+  a.dirw = s.d_dir.get(); a.nwords = s.nwords; a.blkcount = d_cnt.get();
   const unsigned grid = (unsigned)((s.nblocks + kThreads - 1) / kThreads);
   dispatch_nod(NOD, [&](auto c) { k_gen_mark<decltype(c)::value><<<grid, kThreads, 0, st>>>(a); });
   check_launch("k_gen_mark");
-  const uint64_t D = scan_directory(d_cnt.get(), s.nblocks, s.d_dir.get(), st);
-  QS3G_REQUIRE(D < (1ull << 32), QS3G_ERANGE, "sector dimension exceeds 2^32");
+  const uint64_t D = scan_directory(d_cnt.get(), s.nblocks, s.d_dir.get(), s.nwords, st);
+  QS3G_REQUIRE(D < (1ull << 31), QS3G_ERANGE, "sector dimension exceeds 2^31");
   s.D = (int64_t)D;
   s.d_list_s.alloc(D); s.d_list_r.alloc(D); s.d_list_r32.alloc(D); s.d_conf.alloc(D);
-  if (D == 0) return;
+  if (D == 0) { compute_diag(m, s, st); return; }
   DevBuf<double2> d_coef(D);
   DevBuf<int> d_count(D);
   a.list_s = s.d_list_s.get(); a.conf = s.d_conf.get(); a.coef = d_coef.get(); a.count = d_count.get();
@@ -578,6 +603,7 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
   }
   QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_list_r.get(), hr.data(), D * 8, cudaMemcpyHostToDevice, st));
   QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_list_r32.get(), hr32.data(), D * 4, cudaMemcpyHostToDevice, st));
+  compute_diag(m, s, st);
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
 }
 

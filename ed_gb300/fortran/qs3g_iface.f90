@@ -1,0 +1,90 @@
+! qs3g_iface.f90 -- iso_c_binding interface of libqs3g.so for the QS3 Fortran
+! sources.  A QS3 build links -lqs3g and `use qs3g_iface`; the bodies of the
+! routines listed in each comment are then replaced by these calls (see
+! INTEGRATION.md).  Every function returns 0 on success.  Scalars are passed
+! by reference, arrays as Fortran arrays (contiguous, column-major).
+module qs3g_iface
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: QS3G_OK = 0, QS3G_HOST = 0, QS3G_DEVICE = 1
+
+  interface
+    ! state set up by read_ip / get_combination / mk_shift_*_SQ
+    integer(c_int) function qs3g_create(h, NOS, LX, LY, LZ, NOxxz, p_xxz, sJint) bind(C, name="qs3g_create")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr) :: h
+      integer(c_int) :: NOS, LX, LY, LZ, NOxxz
+      integer(c_int) :: p_xxz(2, *)
+      real(c_double) :: sJint(*)          ! sJint(1:NOxxz, 2:3) flattened column-major
+    end function
+
+    integer(c_int) function qs3g_destroy(h) bind(C, name="qs3g_destroy")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: h
+    end function
+
+    ! allocate_lists_omp_SQ (+ explist)
+    integer(c_int) function qs3g_build_sector(h, NOD, KX, KY, KZ, D) bind(C, name="qs3g_build_sector")
+      import :: c_ptr, c_int, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int) :: NOD, KX, KY, KZ
+      integer(c_int64_t) :: D
+    end function
+
+    integer(c_int) function qs3g_get_sector(h, list_s, list_r) bind(C, name="qs3g_get_sector")
+      import :: c_ptr, c_int, c_int64_t, c_double
+      type(c_ptr), value :: h
+      integer(c_int64_t) :: list_s(*)
+      real(c_double) :: list_r(*)
+    end function
+
+    ! ham_to_vec_wave_vector(v0, v1, lv, NOD, list_s, list_r, explist)
+    integer(c_int) function qs3g_hv(h, v0, v1, where) bind(C, name="qs3g_hv")
+      import :: c_ptr, c_int, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: v0(*), v1(*)
+      integer(c_int) :: where
+    end function
+
+    ! lancz_eigen_val_complex (TRLan)
+    integer(c_int) function qs3g_trlan(h, NOE, NOK, NOM, maxitr, tol, precision, conv_mode, start_mode, &
+        seed, start, ene, psi, iters, resid) bind(C, name="qs3g_trlan")
+      import :: c_ptr, c_int, c_double, c_double_complex, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int) :: NOE, NOK, NOM, maxitr, precision, conv_mode, start_mode, iters
+      real(c_double) :: tol, ene(*), resid(*)
+      integer(c_int64_t) :: seed
+      complex(c_double_complex) :: start(*), psi(*)
+    end function
+
+    ! lancz_eigen_val (plain Lanczos)
+    integer(c_int) function qs3g_lanczos(h, maxitr, minitr, itrint, tol, start_mode, seed, start, ene, psi, &
+        iters) bind(C, name="qs3g_lanczos")
+      import :: c_ptr, c_int, c_double, c_double_complex, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int) :: maxitr, minitr, itrint, start_mode, iters
+      real(c_double) :: tol, ene
+      integer(c_int64_t) :: seed
+      complex(c_double_complex) :: start(*), psi(*)
+    end function
+
+    ! calcu_Sq_a + calcu_DSF_wavevector, for nq wave vectors at once
+    integer(c_int) function qs3g_dsf(h, psi, ene1, spsmsz, nq, qvec, Spos, itr_dsf, rfield, alpha, beta2, &
+        norm1, E0, nlev) bind(C, name="qs3g_dsf")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: psi(*)
+      real(c_double) :: ene1, qvec(3, *), Spos(3, *), rfield, alpha(*), beta2(*), norm1(*), E0(*)
+      integer(c_int) :: spsmsz, nq, itr_dsf, nlev(*)
+    end function
+
+    ! DSFLan continued fraction
+    integer(c_int) function qs3g_cfrac(nq, ldab, nlev, alpha, beta2, norm1, E0, eta, nomega, omega, compat, S) &
+        bind(C, name="qs3g_cfrac")
+      import :: c_int, c_double
+      integer(c_int) :: nq, ldab, nlev(*), nomega, compat
+      real(c_double) :: alpha(*), beta2(*), norm1(*), E0(*), eta, omega(*), S(*)
+    end function
+  end interface
+end module qs3g_iface

@@ -139,6 +139,14 @@ int qs3g_dsf(qs3g_handle h, const qs3g_cplx* psi, const double* ene1, const int*
              const double* rfield, double* alpha, double* beta2, double* norm1, double* E0,
              int* nlev);
 
+/* The start vector alone for one wave vector qvec(1:3): builds the
+ * (N_down', k+q) sector and returns its dimension D_new, its list_s (may be
+ * NULL) and fn = S^a(q)|psi> before normalisation (may be NULL), as calcu_Sq_a
+ * (source/get_expectation_values.f90:281-377) leaves them.  Call with NULL
+ * arrays first to learn D_new. */
+int qs3g_sq_a(qs3g_handle h, const qs3g_cplx* psi, const int* spsmsz, const double* qvec,
+              const double* Spos, int64_t* D_new, int64_t* list_s_new, qs3g_cplx* fn);
+
 /* Continued fraction S(omega) = -Im G / pi of DSFLan
  * (source_DSFLan/main.f90:52-84) for nq spectra at once on an arbitrary omega
  * grid.  alpha/beta2 are column-major (ldab x nq) with nlev(q) levels used;

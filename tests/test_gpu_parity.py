@@ -197,31 +197,59 @@ def test_lanczos(qs3g):
     h.close()
 
 
-@pytest.mark.parametrize("spsmsz", [1, 2, 3])
-def test_dsf_small(qs3g, spsmsz):
-    L, nod = 14, 3
-    b, jxy, jz = inputs.chain_bonds(L, (1.0, 1.0), None)
+def _dsf_case(spsmsz):
+    # S^+ lowers N_down: start from N_down = 5 so the new sector (N_down = 4,
+    # ~70 rows) is deep enough for 12 well-conditioned recursion levels
+    L, nod = 14, (5 if spsmsz == 1 else 3)
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 0.7), (0.2, 0.1))
     args = (L, L, 1, 1, b, jxy, jz)
     om, osec, h, D = both(args, nod, (0, 0, 0))
     w, V = np.linalg.eigh(osec.dense())
-    psi = V[:, 0]
-    Spos = inputs.chain_positions(L)
+    psi = np.ascontiguousarray(V[:, 0])
     nod_new = {1: nod - 1, 2: nod + 1, 3: nod}[spsmsz]
-    qs = [2 * np.pi * m / L for m in (0, 1, 4, 7)]
+    return L, nod, nod_new, om, osec, h, w, psi
+
+
+def _oracle_new_sector(om, nod_new, q):
+    rk = O.wavevector((0, 0, 0), om.Ls) + np.array([q, 0, 0])
+    D2 = O.lib().ora_build_sector(om.h, nod_new, rk, None, None, 0, 0)
+    ls = np.zeros(D2, np.int64)
+    lr = np.zeros(D2)
+    O.lib().ora_build_sector(om.h, nod_new, rk, ls.ctypes.data, lr.ctypes.data, D2, 0)
+    return O.Sector(om, nod_new, (0, 0, 0), ls, lr, rk=rk)
+
+
+@pytest.mark.parametrize("spsmsz", [1, 2, 3])
+def test_sq_a_start_vectors(qs3g, spsmsz):
+    """calcu_Sq_a: S^a(q)|GS> on the GPU (gather form) equals the oracle's scatter."""
+    L, nod, nod_new, om, osec, h, w, psi = _dsf_case(spsmsz)
+    Spos = inputs.chain_positions(L)
+    for mq in (1, 4, 7, 10):
+        q = 2 * np.pi * mq / L
+        ns = _oracle_new_sector(om, nod_new, q)
+        fo = O.sq_a(spsmsz, osec, ns, (q, 0, 0), Spos, psi)
+        ls, fg = h.sq_a(psi, spsmsz, (q, 0, 0), Spos)
+        np.testing.assert_array_equal(ls, ns.list_s)
+        assert np.abs(fg - fo).max() <= 1e-13 * max(1.0, np.abs(fo).max())
+    h.close()
+
+
+@pytest.mark.parametrize("spsmsz", [1, 2, 3])
+def test_dsf_small(qs3g, spsmsz):
+    L, nod, nod_new, om, osec, h, w, psi = _dsf_case(spsmsz)
+    Spos = inputs.chain_positions(L)
+    mqs = (1, 4, 7, 10)
+    qs = [2 * np.pi * m / L for m in mqs]
     itr = 12
     rfield = 0.1
     g = h.dsf(psi, w[0], spsmsz, [(q, 0, 0) for q in qs], Spos, itr, rfield)
     for iq, q in enumerate(qs):
-        rk = O.wavevector((0, 0, 0), om.Ls) + np.array([q, 0, 0])
-        D2 = O.lib().ora_build_sector(om.h, nod_new, rk, None, None, 0, 0)
-        ls = np.zeros(D2, np.int64)
-        lr = np.zeros(D2)
-        O.lib().ora_build_sector(om.h, nod_new, rk, ls.ctypes.data, lr.ctypes.data, D2, 0)
-        ns = O.Sector(om, nod_new, (0, 0, 0), ls, lr, rk=rk)
+        ns = _oracle_new_sector(om, nod_new, q)
         fn = O.sq_a(spsmsz, osec, ns, (q, 0, 0), Spos, psi)
         a, b2, n1, nl = S.dsf_recursion(ns.hv, fn, itr, rfield, L, nod_new)
         assert g["nlev"][iq] == nl
         np.testing.assert_allclose(g["norm1"][iq], n1, rtol=1e-12)
+        np.testing.assert_allclose(g["E0"][iq], w[0] - rfield * (L / 2 - nod), rtol=1e-14)
         np.testing.assert_allclose(g["alpha"][iq, :nl], a, rtol=1e-8, atol=1e-10)
         np.testing.assert_allclose(g["beta2"][iq, :nl], b2, rtol=1e-8, atol=1e-10)
     h.close()
