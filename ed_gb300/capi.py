@@ -29,7 +29,7 @@ EXPORTS = [
     "qs3g_create", "qs3g_destroy", "qs3g_build_sector", "qs3g_get_sector", "qs3g_hv", "qs3g_hv32",
     "qs3g_connection_table", "qs3g_connection_table_rows", "qs3g_trlan", "qs3g_lanczos", "qs3g_dsf",
     "qs3g_cfrac", "qs3g_last_error", "qs3g_kernel_launches", "qs3g_set_stream", "qs3g_sync",
-    "qs3g_sq_a",
+    "qs3g_sq_a", "qs3g_cfrac_noalloc",
 ]
 
 _lib = None
@@ -271,4 +271,22 @@ def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
     _check(load().qs3g_cfrac(_i(nq), _i(ld), _ptr(nlev), _ptr(alpha), _ptr(beta2), _ptr(norm1),
                              _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega), _i(1 if compat else 0),
                              _ptr(S)))
+    return S
+
+
+def cfrac_noalloc(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
+    """qs3g_cfrac_noalloc: the same continued fraction, staged in the library's
+    static device array instead of allocated buffers (for callers that cannot
+    allocate device memory)."""
+    alpha = np.ascontiguousarray(np.atleast_2d(alpha), np.float64)
+    beta2 = np.ascontiguousarray(np.atleast_2d(beta2), np.float64)
+    nq, ld = alpha.shape
+    nlev = np.ascontiguousarray(np.atleast_1d(nlev), np.int32)
+    norm1 = np.ascontiguousarray(np.atleast_1d(norm1), np.float64)
+    E0 = np.ascontiguousarray(np.atleast_1d(E0), np.float64)
+    omega = np.ascontiguousarray(omega, np.float64)
+    S = np.zeros((nq, len(omega)))
+    _check(load().qs3g_cfrac_noalloc(_i(nq), _i(ld), _ptr(nlev), _ptr(alpha), _ptr(beta2), _ptr(norm1),
+                                     _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega),
+                                     _i(1 if compat else 0), _ptr(S)))
     return S

@@ -332,6 +332,18 @@ int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* al
   });
 }
 
+int qs3g_cfrac_noalloc(const int* nq, const int* ldab, const int* nlev, const double* alpha, const double* beta2,
+                       const double* norm1, const double* E0, const double* eta, const int* nomega,
+                       const double* omega, const int* compat, double* S) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(nq && ldab && nlev && alpha && beta2 && norm1 && E0 && eta && nomega && omega && compat && S,
+                 QS3G_EINVAL, "null argument");
+    QS3G_REQUIRE(*nq >= 1 && *ldab >= 1 && *nomega >= 1, QS3G_EINVAL, "sizes must be >= 1");
+    cfrac_noalloc(*nq, *ldab, nlev, alpha, beta2, norm1, E0, *eta, *nomega, omega, *compat, S);
+    return QS3G_OK;
+  });
+}
+
 const char* qs3g_last_error(qs3g_handle h) {
   if (h) return h->last_error.c_str();
   std::lock_guard<std::mutex> lk(g_err_mu);

@@ -15,6 +15,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "hosteig.h"
 #include "qs3g_device.cuh"
@@ -433,6 +435,69 @@ void cfrac(int nq, int ldab, const int* nlev, const double* alpha, const double*
                                                         d_e.get(), eta, nomega, d_w.get(), compat, d_S.get());
   check_launch("k_cfrac");
   QS3G_CHECK_CUDA(cudaMemcpyAsync(S, d_S.get(), (size_t)nomega * nq * 8, cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---------------------------------------------------------------- continued fraction without allocation
+// For callers that cannot call cudaMalloc: the device copies of the inputs and
+// of S live in one file-scope static device array of kCfracStaticDoubles
+// doubles (4 MiB), which every GPU that loads the library holds until the
+// process exits.  The host name g_cfrac_static is only a host-side stand-in
+// for the array; its device address comes from cudaGetSymbolAddress, taken
+// once per device (with that device current) on the first call on it, so that
+// first call should come before any stream capture.  Every call reuses the
+// same array and leaves the last call's data in it; the kernel writes every
+// element of S it returns, so nothing has to start at zero.  Calls that
+// overlap on the GPU (two host threads, or two processes sharing the array
+// through MPS) race on the array.
+constexpr size_t kCfracStaticDoubles = size_t(1) << 19;
+static __device__ __align__(256) double g_cfrac_static[kCfracStaticDoubles];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_cfrac_static_mu;
+double* g_cfrac_static_ptr[kMaxDevices] = {};
+
+double* cfrac_static_area() {
+  int dev = 0;
+  QS3G_CHECK_CUDA(cudaGetDevice(&dev));
+  QS3G_REQUIRE(dev >= 0 && dev < kMaxDevices, QS3G_ERANGE, "device ordinal beyond 64");
+  std::lock_guard<std::mutex> lk(g_cfrac_static_mu);
+  if (!g_cfrac_static_ptr[dev]) {
+    void* p = nullptr;
+    QS3G_CHECK_CUDA(cudaGetSymbolAddress(&p, g_cfrac_static));
+    g_cfrac_static_ptr[dev] = static_cast<double*>(p);
+  }
+  return g_cfrac_static_ptr[dev];
+}
+
+size_t up32(size_t n) { return (n + 31) & ~size_t(31); }  // keep every region 256-byte aligned
+}  // namespace
+
+void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,
+                   const double* E0, double eta, int nomega, const double* omega, int compat, double* S) {
+  for (int q = 0; q < nq; ++q) QS3G_REQUIRE(nlev[q] >= 1 && nlev[q] <= ldab, QS3G_EINVAL, "nlev out of range");
+  const size_t nab = (size_t)ldab * nq, nS = (size_t)nomega * nq;
+  const size_t o_a = 0, o_b = o_a + up32(nab), o_n = o_b + up32(nab), o_e = o_n + up32(nq), o_w = o_e + up32(nq),
+               o_S = o_w + up32(nomega), o_l = o_S + up32(nS), total = o_l + up32(((size_t)nq + 1) / 2);
+  if (total > kCfracStaticDoubles)
+    throw Error(QS3G_ERANGE, "qs3g_cfrac_noalloc: these sizes need " + std::to_string(total * 8) +
+                                 " bytes of device scratch; the static area holds " +
+                                 std::to_string(kCfracStaticDoubles * 8) + " bytes (use qs3g_cfrac)");
+  double* base = cfrac_static_area();
+  int* d_nlev = reinterpret_cast<int*>(base + o_l);
+  const cudaStream_t st = 0;  // the legacy default stream: no stream is created
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_nlev, nlev, (size_t)nq * 4, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(base + o_a, alpha, nab * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(base + o_b, beta2, nab * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(base + o_n, norm1, (size_t)nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(base + o_e, E0, (size_t)nq * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(base + o_w, omega, (size_t)nomega * 8, cudaMemcpyHostToDevice, st));
+  const int64_t tot = (int64_t)nq * nomega;
+  k_cfrac<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(nq, ldab, d_nlev, base + o_a, base + o_b, base + o_n,
+                                                        base + o_e, eta, nomega, base + o_w, compat, base + o_S);
+  check_launch("k_cfrac(static scratch)");
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(S, base + o_S, nS * 8, cudaMemcpyDeviceToHost, st));
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -54,6 +54,11 @@ int lanczos(const Model& m, const Sector& s, int maxitr, int minitr, int itrint,
 void cfrac(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,
            const double* E0, double eta, int nomega, const double* omega, int compat, double* S, cudaStream_t st);
 
+// The same continued fraction staged in a static device array instead of
+// cudaMalloc'd buffers (see krylov.cu); throws QS3G_ERANGE beyond its size.
+void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,
+                   const double* E0, double eta, int nomega, const double* omega, int compat, double* S);
+
 // DSF (calcu_Sq_a + calcu_DSF_wavevector) for nq wave vectors.
 int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int spsmsz, int nq, const double* qvec,
         const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2, double* norm1, double* E0,

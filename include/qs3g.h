@@ -157,6 +157,21 @@ int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* al
                const double* beta2, const double* norm1, const double* E0, const double* eta,
                const int* nomega, const double* omega, const int* compat, double* S);
 
+/* The continued fraction of qs3g_cfrac, with the same arguments and results,
+ * for callers that cannot call cudaMalloc -- a host code whose own allocator
+ * already owns the GPU's memory, or a solver loop that must not trigger the
+ * device-wide synchronisation cudaMalloc and cudaFree can cause.  It allocates
+ * nothing: inputs and S are staged in one static device array of 4 MiB
+ * (524288 doubles) that every GPU loading the library holds until exit, and
+ * sizes that do not fit are rejected with QS3G_ERANGE.  The first call on a
+ * device looks up that array's device address (make it before any stream
+ * capture); calls that overlap on the GPU share the array and race.  Runs on
+ * the legacy default stream and returns when S is written.  Has no
+ * counterpart in the reference, whose DSFLan runs on the CPU. */
+int qs3g_cfrac_noalloc(const int* nq, const int* ldab, const int* nlev, const double* alpha,
+                       const double* beta2, const double* norm1, const double* E0, const double* eta,
+                       const int* nomega, const double* omega, const int* compat, double* S);
+
 /* Last error message for the handle (or the last global one if h is NULL). */
 const char* qs3g_last_error(qs3g_handle h);
 
