@@ -1,7 +1,8 @@
 """Build libqs3g.so (sm_103a) in-tree with nvcc.
 
 Every .cu file under ed_gb300/csrc compiles in parallel to an object for
-sm_103a only, then links into ed_gb300/_build/libqs3g.so.
+sm_103a only (host-only .cpp files with g++), then links into
+ed_gb300/_build/libqs3g.so.
 """
 from __future__ import annotations
 
@@ -27,14 +28,20 @@ def nvcc() -> str:
     return "nvcc"
 
 
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
+
+
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
-    if verbose:
-        cmd[1:1] = ["-Xptxas", "-v"]
+    if src.endswith(".cpp"):
+        cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-c", src, "-o", obj]
+    else:
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        if verbose:
+            cmd[1:1] = ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"compile failed for {src}:\n{r.stdout}\n{r.stderr}")
     if verbose:
         sys.stderr.write(r.stderr)
     return obj
@@ -42,7 +49,7 @@ def _compile(src: str, verbose: bool) -> str:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     deps = srcs + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         [os.path.join(HERE, "..", "include", "qs3g.h")]
     if not force and os.path.exists(LIB):

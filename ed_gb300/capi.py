@@ -26,10 +26,12 @@ OK, EINVAL, ENOMEM, ENOTCONV, EITERCAP, ECUDA, ESTATE, ERANGE, ENOTSUP, EBREAKDO
 HOST, DEVICE = 0, 1
 
 EXPORTS = [
-    "qs3g_create", "qs3g_destroy", "qs3g_build_sector", "qs3g_get_sector", "qs3g_hv", "qs3g_hv32",
+    "qs3g_create", "qs3g_destroy", "qs3g_build_sector", "qs3g_build_sector_u1", "qs3g_get_sector", "qs3g_hv", "qs3g_hv32",
     "qs3g_connection_table", "qs3g_connection_table_rows", "qs3g_trlan", "qs3g_lanczos", "qs3g_dsf",
     "qs3g_cfrac", "qs3g_last_error", "qs3g_kernel_launches", "qs3g_set_stream", "qs3g_sync",
-    "qs3g_sq_a", "qs3g_cfrac_noalloc",
+    "qs3g_sq_a", "qs3g_cfrac_noalloc", "qs3g_correlations",
+    "qs3g_write_wf", "qs3g_read_wf", "qs3g_write_energy", "qs3g_read_energy",
+    "qs3g_write_alpha_beta", "qs3g_read_alpha_beta", "qs3g_format_real",
 ]
 
 _lib = None
@@ -132,6 +134,14 @@ class Handle:
     def build_sector(self, nod, K=(0, 0, 0)):
         D = C.c_int64()
         _check(load().qs3g_build_sector(self.h, _i(nod), _i(K[0]), _i(K[1]), _i(K[2]), C.byref(D)), self.h)
+        self.D = int(D.value)
+        self.nod = int(nod)
+        return self.D
+
+    def build_sector_u1(self, nod):
+        """All C(NOS, nod) configurations, no translations (qs3g_build_sector_u1)."""
+        D = C.c_int64()
+        _check(load().qs3g_build_sector_u1(self.h, _i(nod), C.byref(D)), self.h)
         self.D = int(D.value)
         self.nod = int(nod)
         return self.D
@@ -258,6 +268,21 @@ def _sq_a(h, psi, spsmsz, qvec, Spos):
 Handle.sq_a = lambda self, psi, spsmsz, qvec, Spos: _sq_a(self, psi, spsmsz, qvec, Spos)
 
 
+def _correlations(h, psi):
+    """(szsz, spsm, lm): szsz[a-1, b-1] = <Sz_a Sz_b>, spsm[a-1, b-1] = <S+_a S-_b>, lm = <Sz_i>."""
+    psi = np.ascontiguousarray(psi, np.complex128)
+    n = h.NOS
+    zz = np.zeros(n * n)
+    pm = np.zeros(n * n, np.complex128)
+    lm = np.zeros(n)
+    _check(load().qs3g_correlations(h.h, _ptr(psi), _ptr(zz), _ptr(pm), _ptr(lm)), h.h)
+    # flat index (a-1) + (b-1)*NOS  ->  [a-1, b-1]
+    return zz.reshape(n, n).T.copy(), pm.reshape(n, n).T.copy(), lm
+
+
+Handle.correlations = _correlations
+
+
 def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
     """DSFLan continued fraction for nq spectra: alpha/beta2 are (nq, ldab)."""
     alpha = np.ascontiguousarray(np.atleast_2d(alpha), np.float64)
@@ -290,3 +315,60 @@ def cfrac_noalloc(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
                                      _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega),
                                      _i(1 if compat else 0), _ptr(S)))
     return S
+
+
+# ---------------------------------------------------------------- result files
+def _path(p):
+    return os.fsencode(p)
+
+
+def write_wf(path, psi):
+    """wf<i>.bin: psi as one Fortran unformatted record of complex(8)."""
+    psi = np.ascontiguousarray(psi, np.complex128)
+    _check(load().qs3g_write_wf(_path(path), C.byref(C.c_int64(psi.size)), _ptr(psi)), None)
+
+
+def read_wf(path, dim):
+    psi = np.zeros(int(dim), np.complex128)
+    _check(load().qs3g_read_wf(_path(path), C.byref(C.c_int64(int(dim))), _ptr(psi)), None)
+    return psi
+
+
+def write_energy(path, ene):
+    ene = np.ascontiguousarray(ene, np.float64)
+    _check(load().qs3g_write_energy(_path(path), _i(ene.size), _ptr(ene)), None)
+
+
+def read_energy(path, noe):
+    ene = np.zeros(int(noe))
+    _check(load().qs3g_read_energy(_path(path), _i(noe), _ptr(ene)), None)
+    return ene
+
+
+def write_alpha_beta(path, alpha, beta2, norm1, E0, sztot, ex_i=1, itr=1, append=True):
+    """alpha_beta_values_*.d lines (3I6, 8e23.15) for levels 1..len(alpha)."""
+    alpha = np.ascontiguousarray(alpha, np.float64)
+    beta2 = np.ascontiguousarray(beta2, np.float64)
+    assert alpha.shape == beta2.shape
+    _check(load().qs3g_write_alpha_beta(_path(path), _i(alpha.size), _i(ex_i), _i(itr), _ptr(alpha), _ptr(beta2),
+                                        C.byref(C.c_double(norm1)), C.byref(C.c_double(E0)),
+                                        C.byref(C.c_double(sztot)), _i(1 if append else 0)), None)
+
+
+def read_alpha_beta(path, cap=4000):
+    """(alpha, beta2, norm1, E0, sztot) as DSFLan's list-directed read sees them."""
+    alpha = np.zeros(cap)
+    beta2 = np.zeros(cap)
+    n1, e0, sz = C.c_double(), C.c_double(), C.c_double()
+    n = C.c_int()
+    _check(load().qs3g_read_alpha_beta(_path(path), _i(cap), _ptr(alpha), _ptr(beta2), C.byref(n1), C.byref(e0),
+                                       C.byref(sz), C.byref(n)), None)
+    k = n.value
+    return alpha[:k].copy(), beta2[:k].copy(), n1.value, e0.value, sz.value
+
+
+def format_real(x, w, d, kind="E"):
+    """Fortran Ew.d (kind 'E') or ESw.d (kind 'ES') of x."""
+    out = C.create_string_buffer(w + 1)
+    _check(load().qs3g_format_real(C.byref(C.c_double(x)), _i(1 if kind == "ES" else 0), _i(w), _i(d), out), None)
+    return out.value.decode()

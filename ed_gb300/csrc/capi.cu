@@ -24,6 +24,14 @@ void set_error(qs3g_ctx* h, const std::string& msg) {
   g_last_error = msg;
 }
 
+}  // namespace
+
+// Message of the last failed handle-free call (file I/O), read back by
+// qs3g_last_error(NULL).
+void qs3g::set_global_error(const std::string& msg) { set_error(nullptr, msg); }
+
+namespace {
+
 template <class F>
 int guarded(qs3g_ctx* h, F&& f) {
   try {
@@ -143,6 +151,17 @@ int qs3g_build_sector(qs3g_handle h, const int* NOD, const int* KX, const int* K
     const int K[3] = {*KX, *KY, *KZ};
     std::unique_ptr<Sector> s(new Sector());
     build_sector(h->model, *NOD, K, *s, h->stream);
+    h->sector = std::move(s);
+    if (D_out) *D_out = h->sector->D;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_build_sector_u1(qs3g_handle h, const int* NOD, int64_t* D_out) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h && NOD, QS3G_EINVAL, "null argument");
+    std::unique_ptr<Sector> s(new Sector());
+    build_sector_u1(h->model, *NOD, *s, h->stream);
     h->sector = std::move(s);
     if (D_out) *D_out = h->sector->D;
     return QS3G_OK;
@@ -329,6 +348,15 @@ int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* al
     }
     cudaStreamDestroy(st);
     return QS3G_OK;
+  });
+}
+
+int qs3g_correlations(qs3g_handle h, const qs3g_cplx* psi, double* szsz, qs3g_cplx* spsm, double* lm) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(psi && szsz && spsm, QS3G_EINVAL, "null argument");
+    return correlations(h->model, s, reinterpret_cast<const double2*>(psi), szsz, reinterpret_cast<double2*>(spsm),
+                        lm, h->stream);
   });
 }
 

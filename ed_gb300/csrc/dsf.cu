@@ -207,6 +207,62 @@ __global__ void k_sq_z(SqArgs a, int anchored, int NOS) {
   a.fn[lp] = out;
 }
 
+// U(1)-only start vectors (source_only_u1/get_expectation_values.f90:100-179),
+// gather form: row lp of the NOD' sector sums psi(l) * exp(-i q.R_i) over the
+// sites i in ascending order, exactly the order in which the reference's
+// outer site loop adds into fn(lp).
+//   S^+: l = lp's configuration with down spin i added (i up in lp)
+//   S^-: l = lp's configuration with down spin i removed (i down in lp)
+//   S^z: l = lp, weight Siz = -1/2 (i down) or +1/2 (i up)
+template <int NODN, int SPSMSZ>
+__global__ void k_sq_u1(SqArgs a, int NOS) {
+  const int64_t lp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (lp >= a.Dn) return;
+  int n[NODN];
+  unpack<NODN>(a.conf_new[lp], a.bits, n);
+  double2 acc = make_double2(0.0, 0.0);
+  if constexpr (SPSMSZ == 1) {
+    constexpr int NOD = NODN + 1;
+    int nxt = 0;  // index into n of the first occupied site >= i
+    for (int i = 1; i <= NOS; ++i) {
+      while (nxt < NODN && n[nxt] < i) ++nxt;
+      if (nxt < NODN && n[nxt] == i) continue;
+      int s[NOD];
+#pragma unroll
+      for (int u = 0; u < NOD; ++u)
+        s[u] = (u < nxt) ? n[u < NODN ? u : NODN - 1] : ((u == nxt) ? i : n[u > 0 ? u - 1 : 0]);
+      const int64_t l = (int64_t)full_index<NOD>(s, a.binom_gs, NOS);
+      const double2 t = cmul(a.psi[l], a.eks[i]);
+      acc.x += t.x;
+      acc.y += t.y;
+    }
+  } else if constexpr (SPSMSZ == 2) {
+    constexpr int NOD = NODN - 1;
+#pragma unroll
+    for (int j = 0; j < NODN; ++j) {
+      int s[NOD > 0 ? NOD : 1];
+#pragma unroll
+      for (int u = 0; u < NOD; ++u) s[u] = n[u < j ? u : u + 1];
+      int64_t l = 0;
+      if constexpr (NOD > 0) l = (int64_t)full_index<NOD>(s, a.binom_gs, NOS);
+      const double2 t = cmul(a.psi[l], a.eks[n[j]]);
+      acc.x += t.x;
+      acc.y += t.y;
+    }
+  } else {
+    const double2 pl = a.psi[lp];
+    int nxt = 0;
+    for (int i = 1; i <= NOS; ++i) {
+      while (nxt < NODN && n[nxt] < i) ++nxt;
+      const double siz = (nxt < NODN && n[nxt] == i) ? -0.5 : 0.5;
+      const double2 t = cmul(make_double2(siz * pl.x, siz * pl.y), a.eks[i]);
+      acc.x += t.x;
+      acc.y += t.y;
+    }
+  }
+  a.fn[lp] = make_double2(a.inv_sqrt_nos * acc.x, a.inv_sqrt_nos * acc.y);
+}
+
 __global__ void k_set_scalar(double2* p, double2 v) { *p = v; }
 
 }  // namespace
@@ -218,10 +274,12 @@ void start_vector(const Model& m, const Sector& gs, const double2* d_psi, int sp
   const int NOD = gs.NOD, NOS = m.NOS;
   QS3G_REQUIRE(spsmsz >= 1 && spsmsz <= 3, QS3G_EINVAL, "spsmsz must be 1, 2 or 3");
   QS3G_REQUIRE(!(spsmsz == 1 && NOD <= 1), QS3G_EINVAL, "S+(q,w) needs NOD >= 2");
-  QS3G_REQUIRE(m.chain || spsmsz == 3, QS3G_ENOTSUP, "S+/S- start vectors are implemented for chains");
+  QS3G_REQUIRE(gs.u1 || m.chain || spsmsz == 3, QS3G_ENOTSUP, "S+/S- start vectors are implemented for chains");
   const int NODn = (spsmsz == 1) ? NOD - 1 : (spsmsz == 2 ? NOD + 1 : NOD);
+  QS3G_REQUIRE(NODn <= NOS, QS3G_EINVAL, "S-(q,w) from the all-down sector");
   double rkn[3] = {gs.rk[0] + qv[0], gs.rk[1] + qv[1], gs.rk[2] + qv[2]};
-  build_sector_rk(m, NODn, rkn, ns, st);
+  if (gs.u1) build_sector_u1(m, NODn, ns, st);
+  else build_sector_rk(m, NODn, rkn, ns, st);
   const int64_t Dn = ns.D;
   fn.alloc(std::max<int64_t>(1, Dn));
   if (Dn == 0) return;
@@ -250,7 +308,19 @@ void start_vector(const Model& m, const Sector& gs, const double2* d_psi, int sp
   a.inv_sqrt_nos = 1.0 / std::sqrt((double)NOS);
   a.fn = fn.get();
   const unsigned grid = (unsigned)((Dn + 127) / 128);
-  if (spsmsz == 2) {
+  if (gs.u1) {
+    dispatch_nod2(NODn, [&](auto c) {
+      constexpr int V = decltype(c)::value;
+      if (spsmsz == 1) {
+        if constexpr (V + 1 <= 8) k_sq_u1<V, 1><<<grid, 128, 0, st>>>(a, NOS);
+      } else if (spsmsz == 2) {
+        k_sq_u1<V, 2><<<grid, 128, 0, st>>>(a, NOS);
+      } else {
+        k_sq_u1<V, 3><<<grid, 128, 0, st>>>(a, NOS);
+      }
+    });
+    check_launch("k_sq_u1");
+  } else if (spsmsz == 2) {
     dispatch_nod2(NODn, [&](auto c) {
       constexpr int V = decltype(c)::value;
       if constexpr (V >= 2) k_sq_minus_chain<V><<<grid, 128, 0, st>>>(a);
@@ -297,7 +367,7 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
   const int NOD = gs.NOD, NOS = m.NOS;
   QS3G_REQUIRE(!(2 * NOD == NOS && spsmsz == 2), QS3G_EINVAL, "S-(q,w) = S+(q,w) in the sztot = 0 sector");
   QS3G_REQUIRE(!(spsmsz == 1 && NOD <= 1), QS3G_EINVAL, "S+(q,w) needs NOD >= 2");
-  QS3G_REQUIRE(m.chain || spsmsz == 3, QS3G_ENOTSUP, "S+/S- start vectors are implemented for chains");
+  QS3G_REQUIRE(gs.u1 || m.chain || spsmsz == 3, QS3G_ENOTSUP, "S+/S- start vectors are implemented for chains");
   const int NODn = (spsmsz == 1) ? NOD - 1 : (spsmsz == 2 ? NOD + 1 : NOD);
   const double sztot = (double)NOS / 2.0 - (double)NOD;
   const double sz_new = (double)NOS / 2.0 - (double)NODn;

@@ -88,15 +88,15 @@ struct Cplx<float2> {
 
 template <int NOD, bool KZERO, class V>
 __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
-                                             const typename Cplx<V>::R* __restrict__ diag,
+                                             const double* __restrict__ diag,
                                              const typename Cplx<V>::R* __restrict__ coefR,
                                              const typename Cplx<V>::R* __restrict__ invR, const V* __restrict__ ph,
-                                             int64_t i) {
+                                             int64_t i, double shift) {
   using R = typename Cplx<V>::R;
   int n[NOD];
   unpack<NOD>(__ldg(a.conf + i), a.bits, n);
   const V xi = x[i];
-  const R di = __ldg(diag + i);
+  const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
   R ax = 0, ay = 0;
 #pragma unroll
   for (int m = 0; m < NOD; ++m) {
@@ -133,15 +133,71 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain64(HvArgs a, const doubl
                                                            double2* __restrict__ y) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
-  hv_chain_row<NOD, KZERO, double2>(a, x, y, a.diag, a.coefR, a.invR, a.chainph, i);
+  hv_chain_row<NOD, KZERO, double2>(a, x, y, a.diag, a.coefR, a.invR, a.chainph, i, 0.0);
 }
 
 template <int NOD, bool KZERO>
 __global__ void __launch_bounds__(kHvThreads) k_hv_chain32(HvArgs a, const float2* __restrict__ x,
-                                                           float2* __restrict__ y) {
+                                                           float2* __restrict__ y, float shift) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
-  hv_chain_row<NOD, KZERO, float2>(a, x, y, a.diag32, a.coefR32, a.invR32, a.chainph32, i);
+  hv_chain_row<NOD, KZERO, float2>(a, x, y, a.diag, a.coefR32, a.invR32, a.chainph32, i, (double)shift);
+}
+
+// ------------------------------------------------------------ U(1)-only kernels
+// source_only_u1/ham2vec_v3.f90:35-65: no representative search; the hop's
+// row is the colex rank of the flipped configuration (inv_list), computed
+// from NOD binomial-table loads.  The diagonal is precomputed as for the
+// (NOD, K) sectors; coefR holds sJxy_b (R = 1).
+template <int NOD, class V>
+__device__ __forceinline__ void hv_u1_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
+                                          const typename Cplx<V>::R* __restrict__ coefR, int64_t i, double shift) {
+  using R = typename Cplx<V>::R;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  const V xi = x[i];
+  const R di = (R)(__ldg(a.diag + i) - shift);
+  R ax = 0, ay = 0;
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int t = e0; t < e1; ++t) {
+      const uint32_t w = __ldg(a.adj + t);
+      const int e = (int)(w & 0xffffu);
+      bool edown = false;
+#pragma unroll
+      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+      if (edown) continue;
+      int o[NOD];
+      move_spin<NOD>(n, m, e, o);
+      const int64_t id = (int64_t)full_index<NOD>(o, a.binom, a.NOS);
+      const V xv = x[id];
+      const R c = __ldg(coefR + (w >> 16) * (NOD + 1));
+      ax = fma(c, xv.x, ax);
+      ay = fma(c, xv.y, ay);
+    }
+  }
+  V out;
+  out.x = fma(di, xi.x, ax);
+  out.y = fma(di, xi.y, ay);
+  y[i] = out;
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_u1_64(HvArgs a, const double2* __restrict__ x,
+                                                         double2* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  hv_u1_row<NOD, double2>(a, x, y, a.coefR, i, 0.0);
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_u1_32(HvArgs a, const float2* __restrict__ x,
+                                                         float2* __restrict__ y, float shift) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  hv_u1_row<NOD, float2>(a, x, y, a.coefR32, i, (double)shift);
 }
 
 // ------------------------------------------------------------ general lattice helpers
@@ -258,7 +314,7 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general64(HvArgs a, const dou
 
 template <int NOD>
 __global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const float2* __restrict__ x,
-                                                             float2* __restrict__ y) {
+                                                             float2* __restrict__ y, float shift) {
   const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= a.D) return;
@@ -315,7 +371,7 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const flo
     }
   }
   if (lane == 0) {
-    const float diag = fmaf(-2.f, sdown - both, (float)a.Sz_all);
+    const float diag = (float)((a.Sz_all - (double)shift) - 2.0 * (double)(sdown - both));
     y[i] = make_float2(fmaf(diag, xi.x, acc.x), fmaf(diag, xi.y, acc.y));
   }
 }
@@ -323,8 +379,9 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const flo
 // ------------------------------------------------------------ connection table
 constexpr int kMaxRowEntries = 64;
 
+// kind: 0 = general lattice, 1 = chain, 2 = U(1) only
 template <int NOD>
-__global__ void __launch_bounds__(128) k_conn(HvArgs a, bool chain, int64_t row0, int64_t row1,
+__global__ void __launch_bounds__(128) k_conn(HvArgs a, int kind, int64_t row0, int64_t row1,
                                               int64_t* counts, const int64_t* offs, int64_t* orow,
                                               int64_t* ocol, int* oell, int* obond, int* overflow) {
   const int64_t i = row0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,7 +404,10 @@ __global__ void __launch_bounds__(128) k_conn(HvArgs a, bool chain, int64_t row0
       move_spin<NOD>(n, m, e, o);
       int64_t id;
       int ellcode;  // chain: translation i; general: tau+1 (0 = identity / minimal)
-      if (chain) {
+      if (kind == 2) {
+        id = (int64_t)full_index<NOD>(o, a.binom, a.NOS);
+        ellcode = 0;
+      } else if (kind == 1) {
         int p[NOD], ell;
         chain_rep<NOD>(o, a.L, a.bits, p, ell);
         id = dir_lookup(a.dir, anchored_index<NOD>(p, a.binomA, a.L));
@@ -381,7 +441,7 @@ __global__ void __launch_bounds__(128) k_conn(HvArgs a, bool chain, int64_t row0
     ocol[w] = ec[u] + 1;
     obond[w] = eb[u] + 1;
     int ti = 0, tj = 0, tk = 0;
-    if (chain) {
+    if (kind == 1) {
       if (ee[u] != 0) { ti = ee[u]; tj = 1; tk = 1; }
     } else if (ee[u] != 0) {
       tau_to_ijk(ee[u] - 1, a, ti, tj, tk);
@@ -448,7 +508,11 @@ void compute_diag(const Model& m, Sector& s, cudaStream_t st) {
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
   if (s.D == 0) return;
   const HvArgs a = make_args(m, s);
-  if (s.anchored) {
+  if (s.u1) {
+    const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+    dispatch_nod(s.NOD, [&](auto c) { k_hv_u1_64<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y); });
+    check_launch("k_hv_u1_64");
+  } else if (s.anchored) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
     dispatch_nod(s.NOD, [&](auto c) {
       if (s.kzero) k_hv_chain64<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
@@ -470,20 +534,26 @@ void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y,
   check_launch("k_hv_general64");
 }
 
-void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st) {
+void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift) {
   if (s.D == 0) return;
   const HvArgs a = make_args(m, s);
-  if (s.anchored) {
+  if (s.u1) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
     dispatch_nod(s.NOD, [&](auto c) {
-      if (s.kzero) k_hv_chain32<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
-      else k_hv_chain32<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      k_hv_u1_32<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+    });
+    check_launch("k_hv_u1_32");
+  } else if (s.anchored) {
+    const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+    dispatch_nod(s.NOD, [&](auto c) {
+      if (s.kzero) k_hv_chain32<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+      else k_hv_chain32<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
     });
     check_launch("k_hv_chain32");
   } else {
     const unsigned grid = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
     dispatch_nod(s.NOD, [&](auto c) {
-      k_hv_general32<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      k_hv_general32<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
     });
     check_launch("k_hv_general32");
   }
@@ -495,12 +565,13 @@ int64_t connection_table_rows(const Model& m, const Sector& s, int64_t row0, int
   const int64_t nr = row1 - row0;
   if (nr == 0) return 0;
   const HvArgs a = make_args(m, s);
+  const int kind = s.u1 ? 2 : (s.anchored ? 1 : 0);
   DevBuf<int64_t> d_cnt(nr);
   DevBuf<int> d_ovf(1);
   QS3G_CHECK_CUDA(cudaMemsetAsync(d_ovf.get(), 0, sizeof(int), st));
   const unsigned grid = (unsigned)((nr + 127) / 128);
   dispatch_nod(s.NOD, [&](auto c) {
-    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, s.anchored, row0, row1, d_cnt.get(), nullptr,
+    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, kind, row0, row1, d_cnt.get(), nullptr,
                                                     nullptr, nullptr, nullptr, nullptr, d_ovf.get());
   });
   check_launch("k_conn(count)");
@@ -519,7 +590,7 @@ int64_t connection_table_rows(const Model& m, const Sector& s, int64_t row0, int
   DevBuf<int> d_ell(3 * nnz), d_bond(nnz);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(d_off.get(), h.data(), nr * 8, cudaMemcpyHostToDevice, st));
   dispatch_nod(s.NOD, [&](auto c) {
-    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, s.anchored, row0, row1, nullptr, d_off.get(),
+    k_conn<decltype(c)::value><<<grid, 128, 0, st>>>(a, kind, row0, row1, nullptr, d_off.get(),
                                                     d_row.get(), d_col.get(), d_ell.get(), d_bond.get(),
                                                     d_ovf.get());
   });

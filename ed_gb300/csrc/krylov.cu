@@ -14,6 +14,8 @@
 // per restart to solve the NOM x NOM Ritz problem.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -300,6 +302,200 @@ __global__ void k_residual(double2* __restrict__ w, const double2* __restrict__ 
     w[i] = make_double2(q[i].x - e * v[i].x, q[i].y - e * v[i].y);
 }
 
+// ---------------------------------------------------------------- complex(4) vectors on the FP32 pipe
+// GB300 issues FP64 at 1/64 of the FP32 rate, and float <-> double conversions
+// go through the FP64 pipe too, so complex(4) Krylov vectors are processed
+// with FP32 instructions only while keeping FP64-class reductions:
+//  * a product of two floats is split exactly into p + e (p = a*b rounded,
+//    e = fma(a, b, -p)), and sums are carried as unevaluated float pairs
+//    (hi, lo) with the TwoSum error-free transformation, so a thread's partial
+//    dot product is accurate to about 2^-44 relative before it is widened to
+//    FP64 for the fixed-order block reduction;
+//  * FP64 scalars (alpha, beta, overlaps, Ritz coefficients) are split into
+//    hi + lo floats, so updates round only once, to the FP32 result.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float p) {
+  const float t = __fadd_rn(hi, p);
+  const float z = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(p, z));
+  hi = t;
+  lo = __fadd_rn(lo, err);
+}
+__device__ __forceinline__ void df_add_prod(float& hi, float& lo, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  df_add(hi, lo, p);
+  lo = __fadd_rn(lo, e);
+}
+__device__ __forceinline__ float2 split(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_dot_part32(const float2* __restrict__ x, const float2* __restrict__ y,
+                                                            int64_t n, double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = x[i], b = y[i];
+    df_add_prod(rh, rl, a.x, b.x);
+    df_add_prod(rh, rl, a.y, b.y);
+    df_add_prod(ih, il, a.x, b.y);
+    df_add_prod(ih, il, -a.y, b.x);
+  }
+  const double2 s = block_sum2(make_double2((double)rh + (double)rl, (double)ih + (double)il), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_nrm_part32(const float2* __restrict__ x, int64_t n, double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  float rh = 0.f, rl = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = x[i];
+    df_add_prod(rh, rl, a.x, a.x);
+    df_add_prod(rh, rl, a.y, a.y);
+  }
+  const double2 s = block_sum2(make_double2((double)rh + (double)rl, 0.0), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_gemv_h_part32(const float2* __restrict__ V, int64_t ldv, int ncols,
+                                                               const float2* __restrict__ w, int64_t n,
+                                                               double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  for (int c0 = 0; c0 < ncols; c0 += 8) {
+    float rh[8], rl[8], ih[8], il[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) rh[k] = rl[k] = ih[k] = il[k] = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      const float2 b = w[i];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (c0 + k < ncols) {
+          const float2 a = V[(int64_t)(c0 + k) * ldv + i];
+          df_add_prod(rh[k], rl[k], a.x, b.x);
+          df_add_prod(rh[k], rl[k], a.y, b.y);
+          df_add_prod(ih[k], il[k], a.x, b.y);
+          df_add_prod(ih[k], il[k], -a.y, b.x);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (c0 + k < ncols) {
+        const double2 s =
+            block_sum2(make_double2((double)rh[k] + (double)rl[k], (double)ih[k] + (double)il[k]), sh);
+        if (threadIdx.x == 0) part[(size_t)(c0 + k) * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// w = q - a v - b u with a, b split into float pairs (one rounding to FP32)
+__global__ void k_lanczos_w32(float2* w, const float2* q, const float2* __restrict__ v, const float2* __restrict__ u,
+                              int64_t n, const double2* a, const double2* b, int real_alpha) {
+  const float2 ar = split(a->x), ai = split(real_alpha ? 0.0 : a->y), br = split(u ? b->x : 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 qv = q[i], vv = v[i];
+    float re = qv.x, im = qv.y;
+    // lo parts first, then hi parts
+    re = fmaf(-ar.y, vv.x, re); re = fmaf(ai.y, vv.y, re);
+    im = fmaf(-ar.y, vv.y, im); im = fmaf(-ai.y, vv.x, im);
+    if (u) {
+      const float2 uv = u[i];
+      re = fmaf(-br.y, uv.x, re); im = fmaf(-br.y, uv.y, im);
+      re = fmaf(-br.x, uv.x, re); im = fmaf(-br.x, uv.y, im);
+    }
+    re = fmaf(-ar.x, vv.x, re); re = fmaf(ai.x, vv.y, re);
+    im = fmaf(-ar.x, vv.y, im); im = fmaf(-ai.x, vv.x, im);
+    w[i] = make_float2(re, im);
+  }
+}
+
+__global__ void k_scale_inv32(float2* x, int64_t n, const double2* s) {
+  const float2 inv = split(1.0 / s->x);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = x[i];
+    x[i] = make_float2(fmaf(v.x, inv.x, v.x * inv.y), fmaf(v.y, inv.x, v.y * inv.y));
+  }
+}
+
+// y += sgn * a * x
+__global__ void k_axpy32(float2* __restrict__ y, const float2* __restrict__ x, int64_t n, const double2* a, double sgn) {
+  const float2 ar = split(sgn * a->x), ai = split(sgn * a->y);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 xv = x[i];
+    float2 yv = y[i];
+    float re = yv.x, im = yv.y;
+    re = fmaf(ar.y, xv.x, re); re = fmaf(-ai.y, xv.y, re);
+    im = fmaf(ar.y, xv.y, im); im = fmaf(ai.y, xv.x, im);
+    re = fmaf(ar.x, xv.x, re); re = fmaf(-ai.x, xv.y, re);
+    im = fmaf(ar.x, xv.y, im); im = fmaf(ai.x, xv.x, im);
+    y[i] = make_float2(re, im);
+  }
+}
+
+// w -= V[:, :ncols] * coef, coef split into float pairs in shared memory
+__global__ void k_gemv_sub32(const float2* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
+                             float2* __restrict__ w, int64_t n) {
+  __shared__ float4 c[128];  // (re hi, re lo, im hi, im lo)
+  for (int k = threadIdx.x; k < ncols; k += blockDim.x) {
+    const float2 r = split(coef[k].x), m = split(coef[k].y);
+    c[k] = make_float4(r.x, r.y, m.x, m.y);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 wv = w[i];
+    float re = wv.x, im = wv.y, rlo = 0.f, ilo = 0.f;
+    for (int k = 0; k < ncols; ++k) {
+      const float2 a = V[(int64_t)k * ldv + i];
+      const float4 ck = c[k];
+      rlo = fmaf(-ck.y, a.x, rlo); rlo = fmaf(ck.w, a.y, rlo);
+      ilo = fmaf(-ck.y, a.y, ilo); ilo = fmaf(-ck.w, a.x, ilo);
+      re = fmaf(-ck.x, a.x, re); re = fmaf(ck.z, a.y, re);
+      im = fmaf(-ck.x, a.y, im); im = fmaf(-ck.z, a.x, im);
+    }
+    w[i] = make_float2(re + rlo, im + ilo);
+  }
+}
+
+// In-place restart for complex(4): double-float accumulation, split C.
+__global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int nom, int nok,
+                                                   const double2* __restrict__ C, int64_t n) {
+  extern __shared__ float4 sm4[];
+  float4* cs = sm4;                                       // [nok][nom] split C
+  float2* tile = reinterpret_cast<float2*>(sm4 + (size_t)nom * nok);  // [nom][32]
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  for (int k = threadIdx.x; k < nom * nok; k += blockDim.x) {
+    const float2 r = split(C[k].x), m = split(C[k].y);
+    cs[k] = make_float4(r.x, r.y, m.x, m.y);
+  }
+  for (int k = threadIdx.x; k < nom * 32; k += blockDim.x) {
+    const int col = k / 32, r = k % 32;
+    const int64_t i = r0 + r;
+    tile[k] = (i < n) ? V[(int64_t)col * ldv + i] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t i = r0 + r;
+  if (i < n) {
+    for (int oc = g; oc < nok; oc += 8) {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int j = 0; j < nom; ++j) {
+        const float2 a = tile[j * 32 + r];
+        const float4 c = cs[(size_t)oc * nom + j];
+        df_add_prod(rh, rl, a.x, c.x);
+        df_add_prod(rh, rl, -a.y, c.z);
+        df_add_prod(ih, il, a.x, c.z);
+        df_add_prod(ih, il, a.y, c.x);
+        rl = fmaf(a.x, c.y, fmaf(-a.y, c.w, rl));
+        il = fmaf(a.x, c.w, fmaf(a.y, c.y, il));
+      }
+      V[(int64_t)oc * ldv + i] = make_float2(rh + rl, ih + il);
+    }
+  }
+}
+
 unsigned stream_grid(int64_t n) {
   const int64_t g = (n + 255) / 256;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
@@ -308,58 +504,76 @@ unsigned stream_grid(int64_t n) {
 }  // namespace
 
 // ================================================================ Vec ops
+// complex(8) vectors use FP64 arithmetic; complex(4) vectors use the FP32-pipe
+// kernels above (error-free products, double-float sums, split scalars).
+template <class T>
+constexpr bool kF32 = std::is_same<T, float2>::value;
+
 template <class T>
 void Ops<T>::dot(const T* x, const T* y, int64_t n, double2* out) {
-  k_dot_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
+  if constexpr (kF32<T>) k_dot_part32<<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
+  else k_dot_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
   check_launch("k_dot_part");
   k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 0);
   check_launch("k_red_final");
 }
 template <class T>
 void Ops<T>::nrm(const T* x, int64_t n, double2* out) {
-  k_nrm_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
+  if constexpr (kF32<T>) k_nrm_part32<<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
+  else k_nrm_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
   check_launch("k_nrm_part");
   k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 1);
   check_launch("k_red_final");
 }
 template <class T>
 void Ops<T>::scale_inv(T* x, int64_t n, const double2* s) {
-  k_scale_inv<T><<<stream_grid(n), 256, 0, st>>>(x, n, s);
+  if constexpr (kF32<T>) k_scale_inv32<<<stream_grid(n), 256, 0, st>>>(x, n, s);
+  else k_scale_inv<T><<<stream_grid(n), 256, 0, st>>>(x, n, s);
   check_launch("k_scale_inv");
 }
 template <class T>
 void Ops<T>::lanczos_w(T* w, const T* q, const T* v, const T* u, int64_t n, const double2* a, const double2* b,
                        bool real_alpha) {
-  k_lanczos_w<T><<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
+  if constexpr (kF32<T>) k_lanczos_w32<<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
+  else k_lanczos_w<T><<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
   check_launch("k_lanczos_w");
 }
 template <class T>
 void Ops<T>::axpy(T* y, const T* x, int64_t n, const double2* a, double sgn) {
-  k_axpy<T><<<stream_grid(n), 256, 0, st>>>(y, x, n, a, sgn);
+  if constexpr (kF32<T>) k_axpy32<<<stream_grid(n), 256, 0, st>>>(y, x, n, a, sgn);
+  else k_axpy<T><<<stream_grid(n), 256, 0, st>>>(y, x, n, a, sgn);
   check_launch("k_axpy");
 }
 template <class T>
 void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov) {
   if (ncols <= 0) return;
-  k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+  if constexpr (kF32<T>) k_gemv_h_part32<<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+  else k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
   check_launch("k_gemv_h_part");
   k_gemv_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, ncols, ov);
   check_launch("k_gemv_final");
-  k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, ov, w, n);
-  check_launch("k_gemv_sub");
+  gemv_sub(V, ldv, ncols, ov, w, n);
 }
 template <class T>
 void Ops<T>::gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n) {
   if (ncols <= 0) return;
-  k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  if constexpr (kF32<T>) k_gemv_sub32<<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  else k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
   check_launch("k_gemv_sub");
 }
 template <class T>
 void Ops<T>::restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int64_t n) {
-  const size_t sm = ((size_t)nom * 32 + (size_t)nom * nok) * sizeof(double2);
-  if (sm > 48 * 1024)
-    QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_restart<T><<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+  if constexpr (kF32<T>) {
+    const size_t sm = (size_t)nom * nok * sizeof(float4) + (size_t)nom * 32 * sizeof(float2);
+    if (sm > 48 * 1024)
+      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_restart32<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+  } else {
+    const size_t sm = ((size_t)nom * 32 + (size_t)nom * nok) * sizeof(double2);
+    if (sm > 48 * 1024)
+      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_restart<T><<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+  }
   check_launch("k_restart");
 }
 template <class T>
@@ -504,18 +718,27 @@ void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const
 // ================================================================ thick-restart Lanczos
 namespace {
 
+// QS3G_VERBOSE=1 prints one progress line per restart, as QS3 does.
+bool verbose() {
+  static const bool v = [] {
+    const char* e = std::getenv("QS3G_VERBOSE");
+    return e && e[0] && e[0] != '0';
+  }();
+  return v;
+}
+
 template <class T>
 struct HvOp;
 template <>
 struct HvOp<double2> {
-  static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
+  static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st, double) {
     hv64(m, s, x, y, st);
   }
 };
 template <>
 struct HvOp<float2> {
-  static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st) {
-    hv32(m, s, x, y, st);
+  static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, double shift) {
+    hv32(m, s, x, y, st, (float)shift);
   }
 };
 
@@ -530,7 +753,8 @@ struct TrlanOut {
 // V must hold NOM+1 columns of length ldv; V[:,0] holds the start vector.
 template <class T>
 TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
-                    double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes) {
+                    double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes,
+                    double shift = 0.0) {
   const int64_t D = s.D;
   Ops<T> ops{st, sc.part.get()};
   double2* alpha = sc.scal;              // [NOM+2]
@@ -547,7 +771,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
   ops.nrm(col(0), D, beta + 0);
   for (int i = 1; i <= NOM; ++i) {
     ops.scale_inv(col(i - 1), D, beta + (i - 1));
-    HvOp<T>::apply(m, s, col(i - 1), Q, st);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     if (i > 1) {
@@ -576,7 +800,8 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
   std::vector<zd> calpha(NOM + 1), cbeta(NOM + 1);
   for (int j = 1; j <= NOM; ++j) calpha[j] = ha[j].x;
   for (int j = 0; j <= NOM; ++j) cbeta[j] = hb[j].x;
-  int flag = 0;
+  int flag = 0, stall = 0;
+  double best_conv = 1e300;
   std::vector<double2> hC((size_t)NOM * NOK);
   for (int tritr = 1; tritr <= maxitr; ++tritr) {
     out.restarts = tritr;
@@ -596,9 +821,16 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
       }
     }
     flag = (max_conv < tol) ? flag + 1 : 0;
+    if (verbose())  // the progress line of eigen_solver.f90:157-158
+      std::printf("tritr, ene(NOK), max_conv, flag: %5d %25.15e %11.1e %5d  (%s, hv=%d)\n", tritr, ene[NOK - 1],
+                  max_conv, flag, sizeof(T) == 8 ? "complex(4)" : "complex(8)", out.hv_count);
     if ((conv_mode == 0 && flag == 2) || (conv_mode != 0 && flag >= 1)) {
       out.converged = true;
       break;
+    }
+    if (conv_mode == 2) {  // complex(4) phase: stop once the residual estimate stagnates at the FP32 floor
+      if (max_conv < 0.95 * best_conv) { best_conv = max_conv; stall = 0; }
+      else if (++stall >= 20) break;
     }
     if (tritr == maxitr) break;
     QS3G_CHECK_CUDA(cudaMemcpyAsync(col(NOK), col(NOM), D * sizeof(T), cudaMemcpyDeviceToDevice, st));
@@ -608,7 +840,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     for (int j = 0; j < NOK; ++j) hcb[j] = make_double2(cbeta[j + 1].real(), cbeta[j + 1].imag());
     QS3G_CHECK_CUDA(cudaMemcpyAsync(cb, hcb.data(), NOK * sizeof(double2), cudaMemcpyHostToDevice, st));
     int i = NOK + 1;
-    HvOp<T>::apply(m, s, col(i - 1), Q, st);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     ops.gemv_sub(V, ldv, NOK, cb, Q, D);
@@ -617,7 +849,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     ops.nrm(col(i), D, beta + i);
     for (i = NOK + 2; i <= NOM; ++i) {
       ops.scale_inv(col(i - 1), D, beta + (i - 1));
-      HvOp<T>::apply(m, s, col(i - 1), Q, st);
+      HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
       ++out.hv_count;
       ops.dot(col(i - 1), Q, D, alpha + i);
       ops.lanczos_w(col(i), Q, col(i - 1), col(i - 2), D, alpha + i, beta + (i - 1), false);
@@ -641,6 +873,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     herm_jacobi(NOM, Tm, ene, Cc);
   }
   out.ene = ene;
+  for (double& e : out.ene) e += shift;  // the Lanczos ran on H - shift
   return out;
 }
 
@@ -681,11 +914,13 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     Ops<float2> o32{st, sc.part.get()};
     if (start64) o32.from64(V32.get(), start64, D);
     else o32.random_start(V32.get(), D, p.seed);
-    const double tol1 = p.tol32 > 0 ? p.tol32 : 1e-5;
+    const double tol1 = p.tol32 > 0 ? p.tol32 : 1e-6;
+    // the complex(4) phase runs on H - sigma, sigma = sum_b Jz_b/4 (the fully polarised energy): the
+    // large common diagonal then does not enter the FP32 rounding of H*v
     TrlanOut r1 = trlan_core<float2>(m, s, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, st, sc,
-                                     p.reorth_passes);
+                                     p.reorth_passes, m.Sz_all);
     hv_total += r1.hv_count;
-    // phase 2 start: sum of the NOE Ritz vectors, widened to FP64
+    // phase 2: FP64 thick-restart Lanczos from the sum of the NOE Ritz vectors
     Ops<double2> o64{st, sc.part.get()};
     f32_to_f64(V64.get(), V32.get(), D, st);
     for (int j = 1; j < NOE; ++j) {
@@ -699,9 +934,46 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     if (start64) QS3G_CHECK_CUDA(cudaMemcpyAsync(V64.get(), start64, D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     else o64.random_start(V64.get(), D, p.seed);
   }
-  TrlanOut r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, p.tol, p.conv_mode,
-                                    st, sc, p.reorth_passes);
-  hv_total += r2.hv_count;
+  const int hv_phase1 = hv_total;
+  // With a residual target (conv_mode 1, 2) the Ritz estimate |beta C| can sit
+  // below the true residual; the run is accepted only when the FP64 residual
+  // ||H psi - E psi|| recomputed from the Ritz vectors meets the target, else it
+  // continues from the current Ritz vectors with a tighter estimate target.
+  double tol_est = p.conv_mode == 0 ? p.tol : 0.5 * p.tol;
+  TrlanOut r2;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st, sc,
+                             p.reorth_passes);
+    hv_total += r2.hv_count;
+    if (p.conv_mode == 0 || !r2.converged) break;
+    Ops<double2> o64{st, sc.part.get()};
+    DevBuf<double2> W(D);
+    double worst = 0.0;
+    for (int j = 0; j < NOE; ++j) {
+      double2* pj = V64.get() + (int64_t)j * ldv;
+      hv64(m, s, pj, Q64.get(), st);
+      residual64(W.get(), Q64.get(), pj, D, r2.ene[j], st);
+      o64.nrm(W.get(), D, sc.scal);
+      double2 rr;
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(&rr, sc.scal, sizeof(double2), cudaMemcpyDeviceToHost, st));
+      QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+      const double scale = p.conv_mode == 2 ? std::max(1.0, std::fabs(r2.ene[j])) : 1.0;
+      worst = std::max(worst, rr.x / scale);
+    }
+    hv_total += NOE;
+    if (verbose()) std::printf("trlan: Ritz estimate met %.2e, recomputed residual %.3e\n", tol_est, worst);
+    if (worst <= p.tol) break;
+    r2.converged = false;
+    tol_est *= std::max(0.01, 0.5 * p.tol / worst);
+    // continue from the Ritz vectors: sum of the NOE lowest as the new start
+    for (int j = 1; j < NOE; ++j) {
+      std::vector<double2> one(1, make_double2(1.0, 0.0));
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, one.data(), sizeof(double2), cudaMemcpyHostToDevice, st));
+      o64.axpy(V64.get(), V64.get() + (int64_t)j * ldv, D, sc.C, 1.0);
+    }
+  }
+  if (verbose()) std::printf("trlan: %d H*v in the complex(4) phase, %d in the complex(8) phase\n", hv_phase1,
+                             hv_total - hv_phase1);
   converged = r2.converged;
   ene = r2.ene;
   for (int j = 0; j < NOE; ++j) ene_out[j] = ene[j];

@@ -69,8 +69,16 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
 int sq_a(const Model& m, const Sector& gs, const double2* h_psi, int spsmsz, const double* qv, const double* Spos,
          int64_t* Dn_out, int64_t* list_s_new, double2* h_fn, cudaStream_t st);
 
+// <Sz_a Sz_b>, <S+_a S-_b> for all NOS^2 ordered pairs and <Sz_i> of the sector
+// vector h_v (get_cf_2_wave_vector / get_lm_2_wave_vector); spsm may be null.
+int correlations(const Model& m, const Sector& s, const double2* h_v, double* szsz, double2* spsm, double* lm,
+                 cudaStream_t st);
+
 // Sector build for an arbitrary wave vector rk (DSF sectors use rk + q).
 void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cudaStream_t st);
+
+// U(1)-only basis: every configuration of NOD down spins, in colex order.
+void build_sector_u1(const Model& m, int NOD, Sector& s, cudaStream_t st);
 
 // H(i,i) for every row of the sector (called by the sector build).
 void compute_diag(const Model& m, Sector& s, cudaStream_t st);

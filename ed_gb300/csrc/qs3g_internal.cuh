@@ -42,6 +42,9 @@ inline void check_launch(const char* what) {
   count_launch();
 }
 
+// Record the message of a failed handle-free call for qs3g_last_error(NULL).
+void set_global_error(const std::string& msg);
+
 // ---------------------------------------------------------------- device buffers
 template <class T>
 struct DevBuf {
@@ -103,6 +106,7 @@ struct Sector {
   int K[3] = {0, 0, 0};
   double rk[3] = {0, 0, 0};
   bool anchored = false;            // chain: reps occupy site 1, directory over C(NOS-1, NOD-1)
+  bool u1 = false;                  // U(1) only: every configuration is a row, row = colex rank - 1
   bool kzero = false;               // every phase equals exp(0) = 1 exactly
   uint64_t nspace = 0;              // candidates in the directory space
   int64_t D = 0;
@@ -137,7 +141,8 @@ struct HvWork {  // scratch for the general-lattice kernel (none needed today)
 };
 
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
-void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st);
+// complex(4) H*v of H - shift (shift = 0 for the plain product)
+void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift = 0.f);
 void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
 
 // connection table: counts per row then entries

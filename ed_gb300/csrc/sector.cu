@@ -399,6 +399,36 @@ void dispatch_nod(int NOD, F&& f) {
   }
 }
 
+// U(1) basis: row i (0-based) is the configuration of colex rank i + 1
+// (list_fly, source_only_u1/state_lists.f90:85-99).  Colex unranking: for
+// j = NOD..1 the site n_j is the largest n with C(n-1, j) <= remaining rank.
+template <int NOD>
+__global__ void __launch_bounds__(kThreads) k_u1_emit(int NOS, int bits, int64_t D, const uint64_t* __restrict__ binom,
+                                                      int64_t* list_s, double* list_r, float* list_r32,
+                                                      uint64_t* conf) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D) return;
+  uint64_t r = (uint64_t)i;
+  int n[NOD];
+  int hi = NOS;
+#pragma unroll
+  for (int j = NOD; j >= 1; --j) {
+    const uint64_t* bj = binom + (size_t)j * (NOS + 1);
+    int lo = j, up = hi;  // n in [j, hi]: C(lo-1, j) = 0 <= r always
+    while (lo < up) {
+      const int mid = (lo + up + 1) >> 1;
+      if (bj[mid - 1] <= r) lo = mid; else up = mid - 1;
+    }
+    n[j - 1] = lo;
+    r -= bj[lo - 1];
+    hi = lo - 1;
+  }
+  conf[i] = pack<NOD>(n, bits);
+  list_s[i] = i + 1;
+  list_r[i] = 1.0;
+  list_r32[i] = 1.0f;
+}
+
 // Exclusive scan of the block counts, folded into the directory; returns the total.
 uint64_t scan_directory(uint32_t* blkcount, uint64_t nblocks, uint2* dirw, uint64_t nwords, cudaStream_t st) {
   const uint64_t nchunks = (nblocks + 1023) / 1024;
@@ -603,6 +633,55 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
   }
   QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_list_r.get(), hr.data(), D * 8, cudaMemcpyHostToDevice, st));
   QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_list_r32.get(), hr32.data(), D * 4, cudaMemcpyHostToDevice, st));
+  compute_diag(m, s, st);
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+// U(1)-only basis: all C(NOS, NOD) configurations, row = colex rank - 1
+// (get_combination + list_fly + inv_list, source_only_u1/state_lists.f90:6-99;
+// THS = combination(NOS, NOD) in source_only_u1/main.f90).  No translations:
+// list_r = 1 and every hop coefficient is sJxy_b.
+void build_sector_u1(const Model& m, int NOD, Sector& s, cudaStream_t st) {
+  QS3G_REQUIRE(NOD >= 1 && NOD <= kMaxNOD, QS3G_ENOTSUP, "NOD must be in [1, 8]");
+  QS3G_REQUIRE(NOD <= m.NOS, QS3G_EINVAL, "NOD > NOS");
+  QS3G_REQUIRE(NOD * m.bits <= 64, QS3G_ERANGE, "NOD * bits(NOS) exceeds one 64-bit word");
+  const uint64_t ths = binom_u64(m.NOS, NOD);
+  QS3G_REQUIRE(ths < (1ull << 31), QS3G_ERANGE, "C(NOS, NOD) exceeds 2^31 rows");
+  s.NOD = NOD;
+  s.u1 = true;
+  s.anchored = false;
+  s.kzero = true;
+  for (int d = 0; d < 3; ++d) { s.K[d] = 0; s.rk[d] = 0.0; }
+  s.nspace = ths;
+  s.D = (int64_t)ths;
+  s.nblocks = 0;
+  s.nwords = 0;
+  const int KB = NOD + 1;
+  std::vector<uint64_t> hb((size_t)(KB + 1) * (m.NOS + 1));
+  for (int k = 0; k <= KB; ++k)
+    for (int n = 0; n <= m.NOS; ++n) hb[(size_t)k * (m.NOS + 1) + n] = binom_u64(n, k);
+  s.d_binom.alloc(hb.size());
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_binom.get(), hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
+  const int64_t D = s.D;
+  s.d_list_s.alloc(D); s.d_list_r.alloc(D); s.d_list_r32.alloc(D); s.d_conf.alloc(D);
+  const unsigned grid = (unsigned)((D + kThreads - 1) / kThreads);
+  dispatch_nod(NOD, [&](auto c) {
+    k_u1_emit<decltype(c)::value><<<grid, kThreads, 0, st>>>(m.NOS, m.bits, D, s.d_binom.get(), s.d_list_s.get(),
+                                                              s.d_list_r.get(), s.d_list_r32.get(), s.d_conf.get());
+  });
+  check_launch("k_u1_emit");
+  // hop coefficients sJxy_b (table layout of the chain kernels, R = 1)
+  std::vector<double> cr((size_t)std::max(1, m.NOxxz) * (NOD + 1), 0.0), ir(NOD + 1, 1.0);
+  std::vector<float> cr32(cr.size()), ir32(NOD + 1, 1.0f);
+  for (int b = 0; b < m.NOxxz; ++b)
+    for (int c = 0; c <= NOD; ++c) cr[(size_t)b * (NOD + 1) + c] = m.sJxy[b];
+  for (size_t k = 0; k < cr.size(); ++k) cr32[k] = (float)cr[k];
+  s.d_coefR.alloc(cr.size()); s.d_coefR32.alloc(cr.size());
+  s.d_invR.alloc(NOD + 1); s.d_invR32.alloc(NOD + 1);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_coefR.get(), cr.data(), cr.size() * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_coefR32.get(), cr32.data(), cr32.size() * 4, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_invR.get(), ir.data(), (NOD + 1) * 8, cudaMemcpyHostToDevice, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(s.d_invR32.get(), ir32.data(), (NOD + 1) * 4, cudaMemcpyHostToDevice, st));
   compute_diag(m, s, st);
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
 }

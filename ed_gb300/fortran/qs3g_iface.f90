@@ -86,5 +86,45 @@ module qs3g_iface
       integer(c_int) :: nq, ldab, nlev(*), nomega, compat
       real(c_double) :: alpha(*), beta2(*), norm1(*), E0(*), eta, omega(*), S(*)
     end function
+
+    ! U(1)-only basis of source_only_u1 (get_combination + list_fly)
+    integer(c_int) function qs3g_build_sector_u1(h, NOD, D) bind(C, name="qs3g_build_sector_u1")
+      import :: c_ptr, c_int, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int) :: NOD
+      integer(c_int64_t) :: D
+    end function
+
+    ! get_cf_2_wave_vector + get_lm_2_wave_vector for all NOS**2 pairs
+    integer(c_int) function qs3g_correlations(h, psi, szsz, spsm, lm) bind(C, name="qs3g_correlations")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: psi(*), spsm(*)
+      real(c_double) :: szsz(*), lm(*)
+    end function
+
+    ! write_wf / read_wf record (path is a NUL-terminated character string)
+    integer(c_int) function qs3g_write_wf(path, dim, psi) bind(C, name="qs3g_write_wf")
+      import :: c_int, c_int64_t, c_char, c_double_complex
+      character(kind=c_char) :: path(*)
+      integer(c_int64_t) :: dim
+      complex(c_double_complex) :: psi(*)
+    end function
+
+    integer(c_int) function qs3g_read_wf(path, dim, psi) bind(C, name="qs3g_read_wf")
+      import :: c_int, c_int64_t, c_char, c_double_complex
+      character(kind=c_char) :: path(*)
+      integer(c_int64_t) :: dim
+      complex(c_double_complex) :: psi(*)
+    end function
+
+    ! alpha_beta_values_*.d lines
+    integer(c_int) function qs3g_write_alpha_beta(path, nlines, ex_i, itr, alpha, beta2, norm1, E0, sztot, &
+        append) bind(C, name="qs3g_write_alpha_beta")
+      import :: c_int, c_char, c_double
+      character(kind=c_char) :: path(*)
+      integer(c_int) :: nlines, ex_i, itr, append
+      real(c_double) :: alpha(*), beta2(*), norm1, E0, sztot
+    end function
   end interface
 end module qs3g_iface

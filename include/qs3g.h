@@ -61,6 +61,17 @@ int qs3g_destroy(qs3g_handle h);
 int qs3g_build_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ,
                       int64_t* D_out);
 
+/* Build the U(1)-only basis of the variant program: all C(NOS, NOD)
+ * configurations, row i = the configuration list_fly(i) of colex rank i, no
+ * translation symmetry.  Replaces get_combination + list_fly + inv_list
+ * (source_only_u1/state_lists.f90:6-99) with THS = combination(NOS, NOD).
+ * qs3g_hv / qs3g_hv32 then act as source_only_u1/ham2vec_v3.f90:35-65, and
+ * qs3g_trlan, qs3g_lanczos, qs3g_connection_table, qs3g_correlations
+ * (source_only_u1/ham2vec_v3.f90:67-141), qs3g_sq_a and qs3g_dsf
+ * (source_only_u1/get_expectation_values.f90:100-391) work on it.
+ * qs3g_get_sector returns list_s(i) = i and list_r(i) = 1. */
+int qs3g_build_sector_u1(qs3g_handle h, const int* NOD, int64_t* D_out);
+
 /* Copy the sector lists to the host: list_s(1:D) (colex ranks, ascending)
  * and list_r(1:D) = sqrt(norm^2), as allocate_lists_omp_SQ leaves them. */
 int qs3g_get_sector(qs3g_handle h, int64_t* list_s, double* list_r);
@@ -147,6 +158,17 @@ int qs3g_dsf(qs3g_handle h, const qs3g_cplx* psi, const double* ene1, const int*
 int qs3g_sq_a(qs3g_handle h, const qs3g_cplx* psi, const int* spsmsz, const double* qvec,
               const double* Spos, int64_t* D_new, int64_t* list_s_new, qs3g_cplx* fn);
 
+/* Static correlations of a sector vector psi (host, D elements, normalised):
+ * szsz(1:NOS**2) = <Sz_a Sz_b> and spsm(1:NOS**2) = <S+_a S-_b> at index
+ * a + (b-1)*NOS for the pair (list_expe_ss(1), list_expe_ss(2)) = (a, b), and
+ * lm(1:NOS) = <Sz_i> (may be NULL).  Replaces get_cf_2_wave_vector +
+ * calcu_cf_trans_2 (source/get_expectation_values.f90:234-279,
+ * source/ham2vec_v3.f90:111-174) for the full pair list (NOCF = NOS**2) and
+ * get_lm_2_wave_vector + calcu_lm_trans_2 (source/get_expectation_values.f90:
+ * 197-232, source/ham2vec_v3.f90:74-109). */
+int qs3g_correlations(qs3g_handle h, const qs3g_cplx* psi, double* szsz, qs3g_cplx* spsm,
+                      double* lm);
+
 /* Continued fraction S(omega) = -Im G / pi of DSFLan
  * (source_DSFLan/main.f90:52-84) for nq spectra at once on an arbitrary omega
  * grid.  alpha/beta2 are column-major (ldab x nq) with nlev(q) levels used;
@@ -171,6 +193,44 @@ int qs3g_cfrac(const int* nq, const int* ldab, const int* nlev, const double* al
 int qs3g_cfrac_noalloc(const int* nq, const int* ldab, const int* nlev, const double* alpha,
                        const double* beta2, const double* norm1, const double* E0, const double* eta,
                        const int* nomega, const double* omega, const int* compat, double* S);
+
+/* ---- result files in the reference's formats (host only, no GPU needed) ----
+ * Byte-compatible with what the Fortran writes, so that a re_wf = 1 restart
+ * and the external DSFLan program read files written here and vice versa.
+ * Errors are reported through qs3g_last_error(NULL). */
+
+/* wf<i>.bin: psi(1:dim) as one Fortran unformatted sequential record of
+ * complex(8) (4-byte record markers; records over 2147483639 bytes split into
+ * subrecords as gfortran does).  Replaces write_wf / read_wf
+ * (source/input_param.f90:119-184); read takes the first dim values of the
+ * record and fails with QS3G_ERANGE if the record is shorter. */
+int qs3g_write_wf(const char* path, const int64_t* dim, const qs3g_cplx* psi);
+int qs3g_read_wf(const char* path, const int64_t* dim, qs3g_cplx* psi);
+
+/* energy.dat: NOE lines in format (2ES24.15): dble(i), ene(i)
+ * (source/input_param.f90:137-142, 170-176). */
+int qs3g_write_energy(const char* path, const int* NOE, const double* ene);
+int qs3g_read_energy(const char* path, const int* NOE, double* ene);
+
+/* alpha_beta_values_*.d: nlines lines in format (3I6, 8e23.15):
+ * ex_i, n, itr, alpha(n), beta2(n), norm1, E0, sztot
+ * (source/get_expectation_values.f90:522-525, 570-573, 595-603).  append != 0
+ * appends as the reference's position='append' does.  Level 1 of the
+ * reference's -tmp.d file is written with an I15 descriptor for the real
+ * sztot (rejected at run time by gfortran); here it has the E23.15 field of
+ * every other line.  The reader is the list-directed read of DSFLan
+ * (source_DSFLan/main.f90:43-48): up to cap levels of alpha and beta2, norm1,
+ * E0 and sztot of the last line, nlines = lines read (QS3G_ERANGE if more
+ * than cap). */
+int qs3g_write_alpha_beta(const char* path, const int* nlines, const int* ex_i, const int* itr,
+                          const double* alpha, const double* beta2, const double* norm1, const double* E0,
+                          const double* sztot, const int* append);
+int qs3g_read_alpha_beta(const char* path, const int* cap, double* alpha, double* beta2, double* norm1,
+                         double* E0, double* sztot, int* nlines);
+
+/* One value in a Fortran edit descriptor: kind 0 = Ew.d, 1 = ESw.d
+ * (1 <= w <= 64).  out receives w characters and a NUL. */
+int qs3g_format_real(const double* x, const int* kind, const int* w, const int* d, char* out);
 
 /* Last error message for the handle (or the last global one if h is NULL). */
 const char* qs3g_last_error(qs3g_handle h);

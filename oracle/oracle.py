@@ -88,6 +88,11 @@ def lib():
         L.ora_chain_sector.restype = C.c_int64
         L.ora_chain_sector.argtypes = [C.c_void_p, C.c_int, f64p, C.c_void_p, C.c_void_p,
                                        C.c_int64, C.c_int]
+        L.ora_u1_hv.argtypes = [C.c_void_p, C.c_int, f64p, f64p, C.c_int64, C.c_int64, C.c_int]
+        L.ora_u1_corr.restype = C.c_int
+        L.ora_u1_corr.argtypes = [C.c_void_p, C.c_int, f64p, f64p, f64p, f64p, C.c_int]
+        L.ora_u1_sq_a.restype = C.c_int
+        L.ora_u1_sq_a.argtypes = [C.c_void_p, C.c_int, C.c_int, f64p, f64p, f64p, f64p]
         L.ora_cfrac.restype = C.c_int
         L.ora_cfrac.argtypes = [C.c_int, f64p, f64p, C.c_double, C.c_double, C.c_double,
                                 C.c_int, f64p, C.c_int, f64p]
@@ -281,6 +286,56 @@ def sq_a(spsmsz, gs: Sector, new: Sector, qvec, Spos, psi, nthreads=0):
                         psi.view(np.float64), fn.view(np.float64), nthreads)
     if rc != 0:
         raise ValueError("oracle: sq_a unsupported arguments")
+    return fn
+
+
+def u1_hv(model: Model, nod, x, nthreads=0):
+    """ham_to_vec_wave_vector of the U(1)-only variant (source_only_u1/ham2vec_v3.f90:35-65)."""
+    D = model.binom(model.NOS, nod)
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    assert x.shape == (D,)
+    y = np.zeros(D, dtype=np.complex128)
+    lib().ora_u1_hv(model.h, nod, x.view(np.float64), y.view(np.float64), 0, D, nthreads)
+    return y
+
+
+def u1_dense(model: Model, nod):
+    """Dense H of the U(1)-only basis (colex order) from unit vectors; small D only."""
+    D = model.binom(model.NOS, nod)
+    H = np.zeros((D, D), dtype=np.complex128)
+    for j in range(D):
+        e = np.zeros(D, dtype=np.complex128)
+        e[j] = 1.0
+        H[:, j] = u1_hv(model, nod, e)
+    return H
+
+
+def u1_corr(model: Model, nod, v, nthreads=0):
+    """calcu_cf / calcu_lm of the U(1)-only variant for all ordered pairs.
+
+    Returns (szsz, spsm, lm) with S[a-1, b-1] for list_ij = (a, b).
+    """
+    n = model.NOS
+    v = np.ascontiguousarray(v, dtype=np.complex128)
+    zz = np.zeros(n * n)
+    pm = np.zeros(n * n, dtype=np.complex128)
+    lm = np.zeros(n)
+    rc = lib().ora_u1_corr(model.h, nod, v.view(np.float64), zz, pm.view(np.float64), lm, nthreads)
+    if rc != 0:
+        raise ValueError("oracle: u1_corr unsupported arguments")
+    return zz.reshape(n, n).T.copy(), pm.reshape(n, n).T.copy(), lm
+
+
+def u1_sq_a(model: Model, spsmsz, nod, qvec, Spos, psi):
+    """calcu_Sq_a of the U(1)-only variant (source_only_u1/get_expectation_values.f90:100-179)."""
+    nodn = nod - 1 if spsmsz == 1 else (nod + 1 if spsmsz == 2 else nod)
+    fn = np.zeros(model.binom(model.NOS, nodn), dtype=np.complex128)
+    psi = np.ascontiguousarray(psi, dtype=np.complex128)
+    rc = lib().ora_u1_sq_a(model.h, spsmsz, nod, np.ascontiguousarray(qvec, np.float64),
+                           np.ascontiguousarray(np.asarray(Spos, np.float64).reshape(-1)),
+                           psi.view(np.float64), fn.view(np.float64))
+    if rc != 0:
+        raise ValueError("oracle: u1_sq_a unsupported arguments")
     return fn
 
 

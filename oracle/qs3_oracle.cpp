@@ -718,6 +718,161 @@ int ora_corr(void* h, int nod, int64_t D, const int64_t* list_s, const double* l
   return 0;
 }
 
+// ---------------------------------------------------------------- U(1)-only variant
+// ham_to_vec_wave_vector of source_only_u1/ham2vec_v3.f90:35-65: row i
+// (0-based) is list_fly(i+1); every antiparallel bond adds
+// sJint(j,2) * v1(inv_list(j_flip_ni(...))) and -sJint(j,3) * v1(i), every
+// parallel bond +sJint(j,3) * v1(i), in bond order.
+void ora_u1_hv(void* h, int nod, const double* v1, double* v0, int64_t row0, int64_t row1, int nthreads) {
+  const Model& m = *(Model*)h;
+  const cplx* x = (const cplx*)v1;
+  cplx* y = (cplx*)v0;
+  const int64_t D = m.C(m.NOS, nod);
+  if (row1 > D) row1 = D;
+  int nt = nthreads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+  for (int64_t i = row0; i < row1; ++i) {
+    int st[64], ni[64];
+    cplx acc = {0.0, 0.0};
+    list_fly(m, i + 1, nod, st);
+    const cplx xi = x[i];
+    for (int j = 0; j < m.NOxxz; ++j) {
+      bool f1 = contains(st, nod, m.p1[j]);
+      bool f2 = contains(st, nod, m.p2[j]);
+      if (f1 != f2) {
+        acc.re = acc.re - m.sJz[j] * xi.re;
+        acc.im = acc.im - m.sJz[j] * xi.im;
+        j_flip_ni(m.p1[j], m.p2[j], st, nod, ni);
+        const int64_t id = inv_list(m, ni, nod) - 1;
+        acc.re = acc.re + m.sJxy[j] * x[id].re;
+        acc.im = acc.im + m.sJxy[j] * x[id].im;
+      } else {
+        acc.re = acc.re + m.sJz[j] * xi.re;
+        acc.im = acc.im + m.sJz[j] * xi.im;
+      }
+    }
+    y[i] = acc;
+  }
+}
+
+// calcu_cf and calcu_lm of source_only_u1/ham2vec_v3.f90:67-141 for every
+// ordered pair (a, b), stored at (a-1) + (b-1)*NOS, and every site.
+// Each pair's row sum runs serially in row order.
+int ora_u1_corr(void* h, int nod, const double* v_, double* szsz, double* spsm_, double* lm, int nthreads) {
+  const Model& m = *(Model*)h;
+  const cplx* v = (const cplx*)v_;
+  cplx* spsm = (cplx*)spsm_;
+  const int NOS = m.NOS;
+  const int64_t D = m.C(NOS, nod);
+  if (nod < 1 || nod > 63) return -1;
+  int nt = nthreads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (int p = 0; p < NOS * NOS; ++p) {
+    const int a = p % NOS + 1, b = p / NOS + 1;
+    int st[64], ni[64];
+    double zz = 0.0;
+    cplx pm = {0.0, 0.0};
+    if (a == b) {
+      zz = 0.25;
+      for (int64_t i = 0; i < D; ++i) {
+        list_fly(m, i + 1, nod, st);
+        if (contains(st, nod, a)) continue;
+        pm.re += v[i].re * v[i].re + v[i].im * v[i].im;
+      }
+    } else {
+      for (int64_t i = 0; i < D; ++i) {
+        list_fly(m, i + 1, nod, st);
+        const bool f1 = contains(st, nod, a), f2 = contains(st, nod, b);
+        const double w = v[i].re * v[i].re + v[i].im * v[i].im;
+        if (!f1 && f2) {
+          zz -= w;
+        } else if (f1 && !f2) {
+          zz -= w;
+          j_flip_ni(std::min(a, b), std::max(a, b), st, nod, ni);
+          const int64_t id = inv_list(m, ni, nod) - 1;
+          const cplx t = cmul({v[i].re, -v[i].im}, v[id]);
+          pm.re += t.re;
+          pm.im += t.im;
+        } else {
+          zz += w;
+        }
+      }
+      zz *= 0.25;
+    }
+    szsz[p] = zz;
+    spsm[p] = pm;
+  }
+  if (lm) {
+    for (int s = 1; s <= NOS; ++s) {
+      int st[64];
+      double e = 0.0;
+      for (int64_t i = 0; i < D; ++i) {
+        list_fly(m, i + 1, nod, st);
+        const double w = v[i].re * v[i].re + v[i].im * v[i].im;
+        e += contains(st, nod, s) ? -w : w;
+      }
+      lm[s - 1] = e * 0.5;
+    }
+  }
+  return 0;
+}
+
+// calcu_Sq_a of source_only_u1/get_expectation_values.f90:100-179 (scatter
+// form, site loop outermost): fn(lp) += psi(l) * exp(-i q.R_i), then
+// fn /= sqrt(NOS).  fn has C(NOS, nod') elements.  Returns 0, or -1 for
+// unsupported arguments.
+int ora_u1_sq_a(void* h, int spsmsz, int nod, const double* qvec3, const double* Spos, const double* psi_,
+                double* fn_) {
+  const Model& m = *(Model*)h;
+  const int NOS = m.NOS;
+  if (spsmsz < 1 || spsmsz > 3 || nod < 1 || nod > 62) return -1;
+  if (spsmsz == 1 && nod <= 1) return -1;
+  const int nodn = spsmsz == 1 ? nod - 1 : (spsmsz == 2 ? nod + 1 : nod);
+  if (nodn > NOS) return -1;
+  const cplx* psi = (const cplx*)psi_;
+  cplx* fn = (cplx*)fn_;
+  const int64_t D = m.C(NOS, nod), Dn = m.C(NOS, nodn);
+  for (int64_t l = 0; l < Dn; ++l) fn[l] = {0.0, 0.0};
+  std::vector<cplx> eks(NOS + 1);
+  for (int i = 1; i <= NOS; ++i) {
+    const double d = qvec3[0] * Spos[3 * (i - 1)] + qvec3[1] * Spos[3 * (i - 1) + 1] +
+                     qvec3[2] * Spos[3 * (i - 1) + 2];
+    eks[i] = {std::cos(d), -std::sin(d)};
+  }
+  int st[64], nd[64];
+  for (int i = 1; i <= NOS; ++i) {
+    for (int64_t l = 0; l < D; ++l) {
+      list_fly(m, l + 1, nod, st);
+      const bool fi = contains(st, nod, i);
+      if (spsmsz == 1 && fi) {          // search_Spi: remove i
+        int w = 0;
+        for (int k = 0; k < nod; ++k) if (st[k] != i) nd[w++] = st[k];
+        const int64_t lp = inv_list(m, nd, nodn) - 1;
+        const cplx t = cmul(psi[l], eks[i]);
+        fn[lp].re += t.re; fn[lp].im += t.im;
+      } else if (spsmsz == 2 && !fi) {  // search_Smi: insert i
+        int w = 0;
+        bool ins = false;
+        for (int k = 0; k < nod; ++k) {
+          if (!ins && st[k] > i) { nd[w++] = i; ins = true; }
+          nd[w++] = st[k];
+        }
+        if (!ins) nd[w++] = i;
+        const int64_t lp = inv_list(m, nd, nodn) - 1;
+        const cplx t = cmul(psi[l], eks[i]);
+        fn[lp].re += t.re; fn[lp].im += t.im;
+      } else if (spsmsz == 3) {
+        const double siz = fi ? -0.5 : 0.5;
+        const cplx t = cmul({siz * psi[l].re, siz * psi[l].im}, eks[i]);
+        fn[l].re += t.re; fn[l].im += t.im;
+      }
+    }
+  }
+  const double sc = 1.0 / std::sqrt((double)NOS);
+  for (int64_t l = 0; l < Dn; ++l) { fn[l].re *= sc; fn[l].im *= sc; }
+  return 0;
+}
+
 // DSFLan continued fraction (source_DSFLan/main.f90:52-84) on an arbitrary
 // omega grid.  alpha[0..N-1], beta[0..N-1] are the file's alpha(n), beta(n)
 // (beta(1) = 0, beta(n) = beta_n^2).  compat = 1 keeps the reference's deepest

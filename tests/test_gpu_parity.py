@@ -271,3 +271,29 @@ def test_cfrac(qs3g):
         for q in range(nq):
             S0 = O.cfrac(alpha[q, :nlev[q]], beta2[q, :nlev[q]], norm1[q], E0[q], 0.05, om, compat)
             np.testing.assert_allclose(S1[q], S0, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", ["chain16", "chain14_k3", "square4x3"])
+def test_correlations(qs3g, case):
+    """get_cf_2_wave_vector / calcu_cf_trans_2 on the GPU equal the oracle for all NOS^2 pairs."""
+    rng = np.random.default_rng(5)
+    if case == "chain16":
+        args, nod, K = make_chain(16, (1.0, 0.5), (0.3, 0.3)), 4, (0, 0, 0)
+    elif case == "chain14_k3":
+        args, nod, K = make_chain(14, (1.0, 1.0), None), 3, (3, 0, 0)
+    else:
+        b, jxy, jz = lattice_bonds(4, 3, 1, "square", rng)
+        args, nod, K = (12, 4, 3, 1, b, jxy, jz), 3, (1, 0, 0)
+    om, osec, h, D = both(args, nod, K)
+    w, V = np.linalg.eigh(osec.dense())
+    psi = np.ascontiguousarray(V[:, 0])
+    zz0, pm0 = osec.corr(psi)
+    zz1, pm1, lm1 = h.correlations(psi)
+    np.testing.assert_allclose(zz1, zz0.T, rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(pm1, pm0.T, rtol=1e-12, atol=1e-13)
+    NOS = args[0]
+    np.testing.assert_allclose(lm1, 0.5 * (1 - 2 * nod / NOS), rtol=1e-12)
+    # sum rule: sum_b <Sz_a Sz_b> = <Sz_a Sz_tot> = Sz_tot^2 / NOS for an Sz_tot eigenstate
+    sz = NOS / 2 - nod
+    np.testing.assert_allclose(zz1.sum(axis=1), sz * sz / NOS, rtol=1e-10)
+    h.close()

@@ -105,6 +105,39 @@ def test_list_fly_inv_list_roundtrip():
         assert m.inv_list(n) == t
 
 
+@pytest.mark.parametrize("LX,LY,nod", [(10, 1, 3), (4, 3, 4)])
+def test_u1_oracle_against_dense_and_k_union(LX, LY, nod):
+    """U(1)-only H*v (source_only_u1/ham2vec_v3.f90:35-65) equals an independent
+    dense H in colex order, its spectrum is the union of the (NOD, k) spectra,
+    and calcu_cf / calcu_lm satisfy the Sz_tot sum rules."""
+    NOS = LX * LY
+    if LY == 1:
+        b, jxy, jz = E.chain_bonds(NOS, (1.0, 0.7), (0.4, 0.2))
+    else:
+        b, jxy, jz = E.square_bonds(LX, LY, (1.0, 0.6))
+    m = O.Model(NOS, LX, LY, 1, b, jxy, jz, kmax=nod + 2)
+    H = O.u1_dense(m, nod)
+    Hd, confs, index = E.u1_hamiltonian(NOS, nod, b, jxy, jz)
+    perm = [index[tuple(m.list_fly(t, nod))] for t in range(1, comb(NOS, nod) + 1)]
+    np.testing.assert_allclose(H, Hd[np.ix_(perm, perm)], rtol=0, atol=1e-14)
+    w = np.linalg.eigvalsh(H)
+    ks = [(kx, ky, 0) for ky in range(LY) for kx in range(LX)]
+    wk = np.sort(np.concatenate([np.linalg.eigvalsh(m.build_sector(nod, k).dense()) for k in ks]))
+    np.testing.assert_allclose(w, wk, rtol=0, atol=1e-12)
+    psi = np.linalg.eigh(H)[1][:, 0]
+    zz, pm, lm = O.u1_corr(m, nod, psi)
+    sz = NOS / 2 - nod
+    # sum_b <Sz_a Sz_b> = <Sz_a Sz_tot> = sz <Sz_a> (psi need not be translation invariant)
+    np.testing.assert_allclose(zz.sum(axis=1), sz * lm, atol=1e-12)
+    np.testing.assert_allclose(lm.sum(), sz, atol=1e-12)
+    # <S+_a S-_a> = P(a up) = 1/2 + <Sz_a>
+    np.testing.assert_allclose(np.diag(pm).real, 0.5 + lm, atol=1e-12)
+    # S^z(q=0)|psi> = Sz_tot |psi> / sqrt(NOS)
+    Spos = np.array([[i % LX, i // LX, 0] for i in range(NOS)], float)
+    fz = O.u1_sq_a(m, 3, nod, (0.0, 0.0, 0.0), Spos, psi)
+    np.testing.assert_allclose(fz, sz * psi / np.sqrt(NOS), atol=1e-13)
+
+
 def test_representative_ell_rule():
     """ell is the first translation (loop order) reaching the minimum, 0 if minimal."""
     L = 12
