@@ -32,7 +32,12 @@ EXPORTS = [
     "qs3g_sq_a", "qs3g_cfrac_noalloc", "qs3g_correlations",
     "qs3g_write_wf", "qs3g_read_wf", "qs3g_write_energy", "qs3g_read_energy",
     "qs3g_write_alpha_beta", "qs3g_read_alpha_beta", "qs3g_format_real",
+    "qs3g_full_hamiltonian", "qs3g_full_diag",
+    "qs3g_mlp_create", "qs3g_mlp_destroy", "qs3g_mlp_params", "qs3g_mlp_add_sample", "qs3g_mlp_clear",
+    "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict",
 ]
+
+MLP_NPARAMS = 35329
 
 _lib = None
 _lock = threading.Lock()
@@ -315,6 +320,93 @@ def cfrac_noalloc(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
                                      _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega),
                                      _i(1 if compat else 0), _ptr(S)))
     return S
+
+
+def _full_hamiltonian(h):
+    """Dense H(i, id) of the current sector (make_full_hamiltonian), shape (D, D)."""
+    H = np.zeros((h.D, h.D), np.complex128, order="F")
+    _check(load().qs3g_full_hamiltonian(h.h, _ptr(H)), h.h)
+    return H
+
+
+def _full_diag(h, want_psi=True):
+    """All eigenpairs (ALG = 3): (ene[D], psi[D, D] with eigenvectors as columns)."""
+    ene = np.zeros(h.D)
+    psi = np.zeros((h.D, h.D), np.complex128, order="F") if want_psi else None
+    _check(load().qs3g_full_diag(h.h, _ptr(ene), _ptr(psi)), h.h)
+    return ene, psi
+
+
+Handle.full_hamiltonian = _full_hamiltonian
+Handle.full_diag = _full_diag
+
+
+# ---------------------------------------------------------------- learned start
+def band_minimum(J1xy, J2xy):
+    """Wave number of the single-magnon band minimum of J1xy cos q + J2xy cos 2q (J1xy > 0)."""
+    if J2xy <= 0.25 * J1xy:
+        return float(np.pi)
+    return float(np.arccos(-J1xy / (4.0 * J2xy)))
+
+
+class Mlp:
+    """The learned start-vector network (qs3g_mlp_*)."""
+
+    def __init__(self, seed=1):
+        self.h = C.c_void_p()
+        _check(load().qs3g_mlp_create(C.byref(self.h), C.byref(C.c_uint64(seed))), None)
+
+    def close(self):
+        if self.h:
+            load().qs3g_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(MLP_NPARAMS)
+        _check(load().qs3g_mlp_params(self.h, _ptr(p), None), None)
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float64)
+        assert p.shape == (MLP_NPARAMS,)
+        _check(load().qs3g_mlp_params(self.h, None, _ptr(p)), None)
+
+    def add_sample(self, handle, psi, delta, j2, q0):
+        psi = np.ascontiguousarray(psi, np.complex128)
+        cond = np.array([delta, j2, q0], np.float64)
+        _check(load().qs3g_mlp_add_sample(self.h, handle.h, _ptr(psi), _ptr(cond)), handle.h)
+
+    def clear(self):
+        _check(load().qs3g_mlp_clear(self.h), None)
+
+    def loss_grad(self):
+        loss = C.c_double()
+        g = np.zeros(MLP_NPARAMS)
+        _check(load().qs3g_mlp_loss_grad(self.h, C.byref(loss), _ptr(g)), None)
+        return loss.value, g
+
+    def train(self, steps, batch, lr, seed=1):
+        losses = np.zeros(max(1, steps))
+        _check(load().qs3g_mlp_train(self.h, _i(steps), C.byref(C.c_int64(batch)), C.byref(C.c_double(lr)),
+                                     C.byref(C.c_uint64(seed)), _ptr(losses)), None)
+        return losses[:steps]
+
+    def align(self):
+        n = C.c_int()
+        _check(load().qs3g_mlp_align(self.h, C.byref(n)), None)
+        return n.value
+
+    def predict(self, handle, delta, j2, q0):
+        cond = np.array([delta, j2, q0], np.float64)
+        v = np.zeros(handle.D, np.complex128)
+        _check(load().qs3g_mlp_predict(self.h, handle.h, _ptr(cond), _ptr(v), _i(HOST)), handle.h)
+        return v
 
 
 # ---------------------------------------------------------------- result files

@@ -9,6 +9,7 @@
 #include <mutex>
 
 #include "krylov.h"
+#include "mlp.h"
 #include "qs3g_internal.cuh"
 
 using namespace qs3g;
@@ -104,6 +105,9 @@ void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int
   up(m.d_sJz, m.sJz);
   up(m.d_Sz_site, m.Sz_site);
   up(m.d_site_xyz, xyz);
+  std::vector<int2> p12(NOxxz);
+  for (int b = 0; b < NOxxz; ++b) p12[b] = make_int2(m.p1[b], m.p2[b]);
+  up(m.d_p12, p12);
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -368,6 +372,128 @@ int qs3g_cfrac_noalloc(const int* nq, const int* ldab, const int* nlev, const do
                  QS3G_EINVAL, "null argument");
     QS3G_REQUIRE(*nq >= 1 && *ldab >= 1 && *nomega >= 1, QS3G_EINVAL, "sizes must be >= 1");
     cfrac_noalloc(*nq, *ldab, nlev, alpha, beta2, norm1, E0, *eta, *nomega, omega, *compat, S);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_full_hamiltonian(qs3g_handle h, qs3g_cplx* ham) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(ham, QS3G_EINVAL, "null argument");
+    const Sector& s = need_sector(h);
+    full_hamiltonian(h->model, s, reinterpret_cast<double2*>(ham), h->stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_full_diag(qs3g_handle h, double* ene, qs3g_cplx* psi) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(ene, QS3G_EINVAL, "null argument");
+    const Sector& s = need_sector(h);
+    full_diag(h->model, s, ene, reinterpret_cast<double2*>(psi), h->stream);
+    return QS3G_OK;
+  });
+}
+
+// ---------------------------------------------------------------- learned start
+}  // extern "C"
+
+struct qs3g_mlp_ctx {
+  std::unique_ptr<qs3g::Mlp> net;
+  cudaStream_t stream = nullptr;
+};
+
+extern "C" {
+
+int qs3g_mlp_create(qs3g_mlp* out, const uint64_t* seed) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(out && seed, QS3G_EINVAL, "null argument");
+    std::unique_ptr<qs3g_mlp_ctx> c(new qs3g_mlp_ctx());
+    QS3G_CHECK_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    try {
+      c->net.reset(new Mlp(*seed));
+    } catch (...) {
+      cudaStreamDestroy(c->stream);
+      throw;
+    }
+    *out = c.release();
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_destroy(qs3g_mlp net) {
+  if (!net) return QS3G_OK;
+  cudaStreamSynchronize(net->stream);
+  cudaStream_t st = net->stream;
+  delete net;
+  if (st) cudaStreamDestroy(st);
+  return QS3G_OK;
+}
+
+int qs3g_mlp_params(qs3g_mlp net, double* get, const double* set) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(net, QS3G_EINVAL, "null network");
+    if (set) net->net->set_params(set, net->stream);
+    if (get) net->net->get_params(get, net->stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_add_sample(qs3g_mlp net, qs3g_handle h, const qs3g_cplx* psi, const double* cond) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(net && psi && cond, QS3G_EINVAL, "null argument");
+    const Sector& s = need_sector(h);
+    net->net->add_sample(h->model, s, reinterpret_cast<const double2*>(psi), cond, h->stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_clear(qs3g_mlp net) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(net, QS3G_EINVAL, "null network");
+    net->net->clear_samples();
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_loss_grad(qs3g_mlp net, double* loss, double* grad) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(net && loss, QS3G_EINVAL, "null argument");
+    *loss = net->net->loss_grad(nullptr, net->net->nreps, net->stream);
+    if (grad) net->net->gradient(grad, net->stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_train(qs3g_mlp net, const int* steps, const int64_t* batch, const double* lr, const uint64_t* seed,
+                   double* losses) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(net && steps && batch && lr && seed, QS3G_EINVAL, "null argument");
+    net->net->train(*steps, *batch, *lr, *seed, losses, net->stream);
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_align(qs3g_mlp net, int* nflipped) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(net, QS3G_EINVAL, "null network");
+    const int n = net->net->align(net->stream);
+    if (nflipped) *nflipped = n;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_mlp_predict(qs3g_mlp net, qs3g_handle h, const double* cond, qs3g_cplx* start, const int* where) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(net && cond && start && where, QS3G_EINVAL, "null argument");
+    const Sector& s = need_sector(h);
+    if (*where == QS3G_DEVICE) {
+      net->net->predict(h->model, s, cond, reinterpret_cast<double2*>(start), h->stream);
+    } else {
+      DevBuf<double2> v(std::max<int64_t>(1, s.D));
+      net->net->predict(h->model, s, cond, v.get(), h->stream);
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(start, v.get(), s.D * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+      QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    }
     return QS3G_OK;
   });
 }

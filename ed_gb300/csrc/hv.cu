@@ -450,6 +450,71 @@ __global__ void __launch_bounds__(128) k_conn(HvArgs a, int kind, int64_t row0, 
   }
 }
 
+// ------------------------------------------------------------ dense H (ALG = 3)
+// make_full_hamiltonian (ham2vec_v3.f90:5-35; source_only_u1/ham2vec_v3.f90:5-33):
+// one thread per row i walks all bonds in list order and accumulates into
+// H(i, i) and H(i, id) in place, so every entry receives its terms in the
+// reference's order.  The thread owns row i, so the read-modify-writes do
+// not race.  kind: 0 = general lattice, 1 = chain, 2 = U(1) only.
+template <int NOD>
+__global__ void __launch_bounds__(128) k_dense(HvArgs a, int kind, const int2* __restrict__ p12, int nbonds,
+                                               double2* H, int64_t ld) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(a.conf[i], a.bits, n);
+  const size_t ex1 = (size_t)a.LX + 1, ex2 = ex1 * ((size_t)a.LY + 1);
+  double2* hii = H + i + i * ld;
+  for (int j = 0; j < nbonds; ++j) {
+    const int2 p = p12[j];
+    int m1 = -1, m2 = -1;
+#pragma unroll
+    for (int u = 0; u < NOD; ++u) {
+      if (n[u] == p.x) m1 = u;
+      if (n[u] == p.y) m2 = u;
+    }
+    const bool f1 = m1 >= 0, f2 = m2 >= 0;
+    if (f1 == f2) {
+      hii->x = hii->x + a.sJz[j];
+      continue;
+    }
+    hii->x = hii->x - a.sJz[j];
+    // j_flip_ni: the down end moves to the up end
+    int o[NOD];
+    if (f1) move_spin<NOD>(n, m1, p.y, o);
+    else move_spin<NOD>(n, m2, p.x, o);
+    int64_t id;
+    double2 e = make_double2(1.0, 0.0);
+    if (kind == 2) {
+      id = (int64_t)full_index<NOD>(o, a.binom, a.NOS);
+    } else if (kind == 1) {
+      int q[NOD], ell;
+      chain_rep<NOD>(o, a.L, a.bits, q, ell);
+      id = dir_lookup(a.dir, anchored_index<NOD>(q, a.binomA, a.L));
+      e = a.chainph[ell];
+    } else {
+      int bt;
+      const uint64_t best = general_rep_serial<NOD>(o, a, bt);
+      int rep[NOD];
+      unpack<NOD>(best, a.bits, rep);
+      id = dir_lookup(a.dir, full_index<NOD>(rep, a.binom, a.NOS));
+      size_t eidx = 0;
+      if (best != pack<NOD>(o, a.bits)) {
+        int ti, tj, tk;
+        tau_to_ijk(bt, a, ti, tj, tk);
+        eidx = (size_t)ti + ex1 * (size_t)tj + ex2 * (size_t)tk;
+      }
+      e = a.explist[eidx];
+    }
+    if (id < 0) continue;
+    // sJint(j,2) * list_r(id) / list_r(i) * explist(ell), left to right
+    const double c = a.sJxy[j] * a.list_r[id] / a.list_r[i];
+    double2* hij = H + i + id * ld;
+    hij->x = hij->x + c * e.x;
+    hij->y = hij->y + c * e.y;
+  }
+}
+
 HvArgs make_args(const Model& m, const Sector& s) {
   HvArgs a{};
   a.D = s.D; a.L = m.NOS; a.NOS = m.NOS; a.bits = m.bits;
@@ -493,6 +558,19 @@ __global__ void k_diag(HvArgs a, double* diag, float* diag32) {
 }
 
 }  // namespace
+
+void dense_hamiltonian(const Model& m, const Sector& s, double2* H, int64_t ld, cudaStream_t st) {
+  QS3G_REQUIRE(ld >= s.D, QS3G_EINVAL, "leading dimension below D");
+  if (s.D == 0) return;
+  QS3G_CHECK_CUDA(cudaMemsetAsync(H, 0, (size_t)ld * (size_t)s.D * sizeof(double2), st));
+  const HvArgs a = make_args(m, s);
+  const int kind = s.u1 ? 2 : (s.anchored ? 1 : 0);
+  const unsigned grid = (unsigned)((s.D + 127) / 128);
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_dense<decltype(c)::value><<<grid, 128, 0, st>>>(a, kind, m.d_p12.get(), m.NOxxz, H, ld);
+  });
+  check_launch("k_dense");
+}
 
 void compute_diag(const Model& m, Sector& s, cudaStream_t st) {
   s.d_diag.alloc(std::max<int64_t>(1, s.D));

@@ -80,6 +80,10 @@ void build_sector_rk(const Model& m, int NOD, const double rk[3], Sector& s, cud
 // U(1)-only basis: every configuration of NOD down spins, in colex order.
 void build_sector_u1(const Model& m, int NOD, Sector& s, cudaStream_t st);
 
+// ALG = 3: dense H to the host, and all eigenpairs via cuSOLVER zheevd.
+void full_hamiltonian(const Model& m, const Sector& s, double2* h_H, cudaStream_t st);
+void full_diag(const Model& m, const Sector& s, double* h_ene, double2* h_psi, cudaStream_t st);
+
 // H(i,i) for every row of the sector (called by the sector build).
 void compute_diag(const Model& m, Sector& s, cudaStream_t st);
 

@@ -97,6 +97,7 @@ struct Model {
   DevBuf<uint32_t> d_adj;
   DevBuf<double> d_sJxy, d_sJz, d_Sz_site;
   DevBuf<int16_t> d_site_xyz;       // (x, y, z, pad) 0-based per site, index 1..NOS
+  DevBuf<int2> d_p12;               // (p1, p2) per bond, bond order (dense H build)
 };
 
 // ---------------------------------------------------------------- sector
@@ -144,6 +145,10 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
 // complex(4) H*v of H - shift (shift = 0 for the plain product)
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift = 0.f);
 void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+
+// dense H(i, id) of make_full_hamiltonian, column-major with leading dimension ld
+// (zeroed here), accumulated in the reference's bond order
+void dense_hamiltonian(const Model& m, const Sector& s, double2* H, int64_t ld, cudaStream_t st);
 
 // connection table: counts per row then entries
 int64_t connection_table(const Model& m, const Sector& s, int64_t* row, int64_t* col, int* ell,

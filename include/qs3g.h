@@ -194,6 +194,21 @@ int qs3g_cfrac_noalloc(const int* nq, const int* ldab, const int* nlev, const do
                        const double* beta2, const double* norm1, const double* E0, const double* eta,
                        const int* nomega, const double* omega, const int* compat, double* S);
 
+/* ALG = 3, first half: the dense sector Hamiltonian Ham(i, id), D x D
+ * column-major complex(8) (host), built on the GPU with the bonds visited in
+ * list order as make_full_hamiltonian does (source/ham2vec_v3.f90:5-35;
+ * source_only_u1/ham2vec_v3.f90:5-33 for a U(1)-only sector).  D <= 46340. */
+int qs3g_full_hamiltonian(qs3g_handle h, qs3g_cplx* ham);
+
+/* ALG = 3: all eigenpairs of the current sector.  Replaces Full_diag_routines +
+ * fulldia_routines_with_momentum (source/eigen_solver.f90:51-67, 261-337):
+ * the dense H is built on the GPU and diagonalised with cuSOLVER zheevd on its
+ * upper triangle (the reference's zheev('V','U')).  ene(1:D) ascending;
+ * psi(1:D,1:D) (host, may be NULL) the eigenvectors as columns, unique only up
+ * to a phase (and within degenerate levels).  cuSOLVER is loaded at run time;
+ * QS3G_ENOTSUP if it is absent. */
+int qs3g_full_diag(qs3g_handle h, double* ene, qs3g_cplx* psi);
+
 /* ---- result files in the reference's formats (host only, no GPU needed) ----
  * Byte-compatible with what the Fortran writes, so that a re_wf = 1 restart
  * and the external DSFLan program read files written here and vice versa.
@@ -231,6 +246,53 @@ int qs3g_read_alpha_beta(const char* path, const int* cap, double* alpha, double
 /* One value in a Fortran edit descriptor: kind 0 = Ew.d, 1 = ESw.d
  * (1 <= w <= 64).  out receives w characters and a NUL. */
 int qs3g_format_real(const double* x, const int* kind, const int* w, const int* d, char* out);
+
+/* ---- learned start vector (no counterpart in the reference) ----
+ * The reference starts thick-restart Lanczos from a random vector
+ * (source/eigen_solver.f90:92-96).  This network maps the gaps between
+ * consecutive down spins of a chain representative (NOD <= 4) to its k = 0
+ * ground-state amplitude; its prediction is passed to qs3g_trlan with
+ * start_mode = 1.  Layers 16 -> 128 -> 128 -> 128 -> 1 with tanh; parameters
+ * kept in FP32 and used rounded to BF16, products accumulated in FP32; trained
+ * on the GPU by the library's own forward and backward kernels on ground
+ * states that qs3g_trlan produced.  cond = {Delta, J2, q0}: the anisotropy
+ * Jz/Jxy, the next-nearest coupling and the wave number of the magnon band
+ * minimum (pi for J2 <= 1/4, acos(-1/(4 J2)) above), which enter the inputs
+ * as Delta, J2 and cos/sin(q0 * gap).  Parameters are QS3G_MLP_NPARAMS
+ * doubles in the order W1[16][128] b1 W2[128][128] b2 W3[128][128] b3
+ * w4[128] b4. */
+typedef struct qs3g_mlp_ctx* qs3g_mlp;
+#define QS3G_MLP_NPARAMS 35329
+
+/* New network with seeded uniform (Glorot) weights and zero biases. */
+int qs3g_mlp_create(qs3g_mlp* net, const uint64_t* seed);
+int qs3g_mlp_destroy(qs3g_mlp net);
+
+/* Copy the parameters out (get != NULL) and/or in (set != NULL; resets Adam). */
+int qs3g_mlp_params(qs3g_mlp net, double* get, const double* set);
+
+/* Add the k = 0 ground state psi (host, D elements) of the handle's current
+ * chain sector to the training set, with its cond.  Targets are
+ * psi_r * list_r(r) / L * sqrt(C(L, NOD)) after a global phase fix. */
+int qs3g_mlp_add_sample(qs3g_mlp net, qs3g_handle h, const qs3g_cplx* psi, const double* cond);
+int qs3g_mlp_clear(qs3g_mlp net);
+
+/* Mean squared error over the whole training set and its gradient
+ * (QS3G_MLP_NPARAMS doubles, may be NULL) at the current parameters. */
+int qs3g_mlp_loss_grad(qs3g_mlp net, double* loss, double* grad);
+
+/* steps Adam steps on batches of `batch` representatives drawn with
+ * replacement from the seed; losses (may be NULL) receives each batch loss. */
+int qs3g_mlp_train(qs3g_mlp net, const int* steps, const int64_t* batch, const double* lr, const uint64_t* seed,
+                   double* losses);
+
+/* Flip the sign of every training sample whose targets point against the
+ * current network output (the ground state's global sign is arbitrary). */
+int qs3g_mlp_align(qs3g_mlp net, int* nflipped);
+
+/* Start vector for the handle's current chain sector (k = 0):
+ * v_r = f(r) * L / list_r(r), unnormalised, host or device (where). */
+int qs3g_mlp_predict(qs3g_mlp net, qs3g_handle h, const double* cond, qs3g_cplx* start, const int* where);
 
 /* Last error message for the handle (or the last global one if h is NULL). */
 const char* qs3g_last_error(qs3g_handle h);
