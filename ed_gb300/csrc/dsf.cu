@@ -374,6 +374,10 @@ int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int
   const int64_t D = gs.D;
   DevBuf<double2> d_psi(D);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(d_psi.get(), h_psi, D * sizeof(double2), cudaMemcpyHostToDevice, st));
+  // chains: all q in lock step (batch.cu); other lattices and U(1) sectors: one q at a time
+  if (gs.anchored && !gs.u1)
+    return dsf_batched(m, gs, d_psi.get(), ene1, spsmsz, nq, qvec, Spos, itr_dsf, rfield, alpha, beta2, norm1, E0,
+                       nlev, st);
   Scratch sc;
   sc.ensure(8);
   Ops<double2> ops{st, sc.part.get()};

@@ -144,6 +144,28 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain32(HvArgs a, const float
   hv_chain_row<NOD, KZERO, float2>(a, x, y, a.diag, a.coefR32, a.invR32, a.chainph32, i, (double)shift);
 }
 
+// ------------------------------------------------------------ batches of chain sectors
+// Block b works on segment blk_seg[b], rows (b - blk_first[b]) * 256 + tid of
+// it; the segment's tables replace the handle's in the row function.
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain64_seg(const HvSeg* __restrict__ segs,
+                                                               const int* __restrict__ blk_seg,
+                                                               const int* __restrict__ blk_first,
+                                                               const double2* __restrict__ x,
+                                                               double2* __restrict__ y, double shift) {
+  const int sg = blk_seg[blockIdx.x];
+  const HvSeg& g = segs[sg];
+  const int64_t i = (int64_t)(blockIdx.x - blk_first[blockIdx.x]) * blockDim.x + threadIdx.x;
+  if (i >= g.D) return;
+  HvArgs a{};
+  a.D = g.D; a.L = g.L; a.NOS = g.L; a.bits = g.bits;
+  a.conf = g.conf; a.dir = g.dir; a.binomA = g.binomA; a.adj_off = g.adj_off; a.adj = g.adj;
+  const double2* xs = x + g.row0;
+  double2* ys = y + g.row0;
+  if (g.kzero) hv_chain_row<NOD, true, double2>(a, xs, ys, g.diag, g.coefR, g.invR, g.chainph, i, shift);
+  else hv_chain_row<NOD, false, double2>(a, xs, ys, g.diag, g.coefR, g.invR, g.chainph, i, shift);
+}
+
 // ------------------------------------------------------------ U(1)-only kernels
 // source_only_u1/ham2vec_v3.f90:35-65: no representative search; the hop's
 // row is the colex rank of the flipped configuration (inv_list), computed
@@ -558,6 +580,25 @@ __global__ void k_diag(HvArgs a, double* diag, float* diag32) {
 }
 
 }  // namespace
+
+HvSeg make_seg(const Model& m, const Sector& s, int64_t row0) {
+  QS3G_REQUIRE(s.anchored && !s.u1, QS3G_ENOTSUP, "batched H*v serves chain sectors");
+  HvSeg g{};
+  g.D = s.D; g.row0 = row0; g.L = m.NOS; g.bits = m.bits; g.kzero = s.kzero ? 1 : 0;
+  g.conf = s.d_conf.get(); g.dir = s.d_dir.get(); g.binomA = s.d_binomA.get();
+  g.adj_off = m.d_adj_off.get(); g.adj = m.d_adj.get();
+  g.diag = s.d_diag.get(); g.coefR = s.d_coefR.get(); g.invR = s.d_invR.get(); g.chainph = s.d_chainph.get();
+  return g;
+}
+
+void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
+              const double2* x, double2* y, double shift, cudaStream_t st) {
+  if (nblk == 0) return;
+  dispatch_nod(NOD, [&](auto c) {
+    k_hv_chain64_seg<decltype(c)::value><<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y, shift);
+  });
+  check_launch("k_hv_chain64_seg");
+}
 
 void dense_hamiltonian(const Model& m, const Sector& s, double2* H, int64_t ld, cudaStream_t st) {
   QS3G_REQUIRE(ld >= s.D, QS3G_EINVAL, "leading dimension below D");

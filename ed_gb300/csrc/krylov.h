@@ -37,6 +37,30 @@ struct Ops {
 void f32_to_f64(double2* y, const float2* x, int64_t n, cudaStream_t st);
 void residual64(double2* w, const double2* q, const double2* v, int64_t n, double e, cudaStream_t st);
 
+// One chain sector of a batch: everything the chain H*v row needs, with the
+// sector's rows stored at x[row0 .. row0 + D) of the batch's vectors.
+struct HvSeg {
+  int64_t D, row0;
+  int L, bits, kzero, pad;
+  const uint64_t* conf;
+  const uint2* dir;
+  const uint32_t* binomA;
+  const int* adj_off;
+  const uint32_t* adj;
+  const double* diag;
+  const double* coefR;
+  const double* invR;
+  const double2* chainph;
+};
+
+HvSeg make_seg(const Model& m, const Sector& s, int64_t row0);
+
+// H*v - shift*v over a batch of chain sectors with the same NOD: one launch,
+// block b serves segment blk_seg[b] (blocks of 256 rows, each segment padded
+// to whole blocks).
+void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
+              const double2* x, double2* y, double shift, cudaStream_t st);
+
 struct TrlanParams {
   int NOE = 1, NOK = 2, NOM = 4, maxitr = 1000;
   double tol = 1e-12;
@@ -63,6 +87,12 @@ void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const
 int dsf(const Model& m, const Sector& gs, const double2* h_psi, double ene1, int spsmsz, int nq, const double* qvec,
         const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2, double* norm1, double* E0,
         int* nlev, cudaStream_t st);
+
+// The same recursion for all nq wave vectors in lock step on chain sectors
+// (batch.cu); d_psi is the ground state on the device.
+int dsf_batched(const Model& m, const Sector& gs, const double2* d_psi, double ene1, int spsmsz, int nq,
+                const double* qvec, const double* Spos, int itr_dsf, double rfield, double* alpha, double* beta2,
+                double* norm1, double* E0, int* nlev, cudaStream_t st);
 
 // calcu_Sq_a alone for one wave vector: D' of the new sector, its list_s and
 // fn = S^a(q)|psi> before normalisation (host arrays may be null).

@@ -297,3 +297,30 @@ def test_correlations(qs3g, case):
     sz = NOS / 2 - nod
     np.testing.assert_allclose(zz1.sum(axis=1), sz * sz / NOS, rtol=1e-10)
     h.close()
+
+
+def test_dsf_all_q_batched(qs3g):
+    """Every q of a chain at once (one batched recursion): each q equals the
+    oracle's own per-q recursion, and a sweep of one q equals the same q
+    inside the full sweep bit for bit (results do not depend on the batch)."""
+    L, nod = 24, 3
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 1.0))
+    om, osec, h, D = both((L, L, 1, 1, b, jxy, jz), nod, (0, 0, 0))
+    w, V = np.linalg.eigh(osec.dense())
+    psi = np.ascontiguousarray(V[:, 0])
+    Spos = inputs.chain_positions(L)
+    qs = [2 * np.pi * m / L for m in range(L)]
+    itr = 40
+    g = h.dsf(psi, w[0], 2, [(q, 0, 0) for q in qs], Spos, itr, 0.0)
+    for m in (0, 1, 5, 12, 23):
+        ns = _oracle_new_sector(om, nod + 1, qs[m])
+        fn = O.sq_a(2, osec, ns, (qs[m], 0, 0), Spos, psi)
+        a, b2, n1, nl = S.dsf_recursion(ns.hv, fn, itr, 0.0, L, nod + 1)
+        assert g["nlev"][m] == nl
+        np.testing.assert_allclose(g["norm1"][m], n1, rtol=1e-12)
+        np.testing.assert_allclose(g["alpha"][m, :nl], a, rtol=1e-8, atol=1e-10)
+        np.testing.assert_allclose(g["beta2"][m, :nl], b2, rtol=1e-8, atol=1e-10)
+        one = h.dsf(psi, w[0], 2, [(qs[m], 0, 0)], Spos, itr, 0.0)
+        np.testing.assert_array_equal(one["alpha"][0], g["alpha"][m])
+        np.testing.assert_array_equal(one["beta2"][0], g["beta2"][m])
+    h.close()
