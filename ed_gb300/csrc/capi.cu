@@ -289,7 +289,7 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
     p.precision = precision ? *precision : 0;
     p.conv_mode = conv_mode ? *conv_mode : 0;
     p.seed = seed ? *seed : 1;
-    QS3G_REQUIRE(p.precision == 0 || p.precision == 1, QS3G_EINVAL, "precision must be 0 or 1");
+    QS3G_REQUIRE(p.precision >= 0 && p.precision <= 2, QS3G_EINVAL, "precision must be 0, 1 or 2");
     QS3G_REQUIRE(p.conv_mode >= 0 && p.conv_mode <= 2, QS3G_EINVAL, "conv_mode must be 0, 1 or 2");
     const int sm = start_mode ? *start_mode : 0;
     QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");

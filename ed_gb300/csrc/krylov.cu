@@ -185,19 +185,17 @@ __global__ void __launch_bounds__(kRedThreads) k_gemv_h_part(const T* __restrict
   }
 }
 
-// out[c] = sgn * sum_b part[c*nb + b]
+// out[c] = sum_b part[c*nb + b]: one block per column, fixed-order tree
 __global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part, int nb, int ncols, double2* out) {
   __shared__ double2 sh[kRedThreads];
-  for (int c = 0; c < ncols; ++c) {
-    double2 acc = make_double2(0.0, 0.0);
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-      acc.x += part[(size_t)c * nb + i].x;
-      acc.y += part[(size_t)c * nb + i].y;
-    }
-    const double2 s = block_sum2(acc, sh);
-    if (threadIdx.x == 0) out[c] = s;
-    __syncthreads();
+  const int c = blockIdx.x;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    acc.x += part[(size_t)c * nb + i].x;
+    acc.y += part[(size_t)c * nb + i].y;
   }
+  const double2 s = block_sum2(acc, sh);
+  if (threadIdx.x == 0) out[c] = s;
 }
 
 // w -= V[:, :ncols] * coef   (coef from device memory)
@@ -358,38 +356,6 @@ __global__ void __launch_bounds__(kRedThreads) k_nrm_part32(const float2* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_gemv_h_part32(const float2* __restrict__ V, int64_t ldv, int ncols,
-                                                               const float2* __restrict__ w, int64_t n,
-                                                               double2* part) {
-  __shared__ double2 sh[kRedThreads];
-  for (int c0 = 0; c0 < ncols; c0 += 8) {
-    float rh[8], rl[8], ih[8], il[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) rh[k] = rl[k] = ih[k] = il[k] = 0.f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-      const float2 b = w[i];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        if (c0 + k < ncols) {
-          const float2 a = V[(int64_t)(c0 + k) * ldv + i];
-          df_add_prod(rh[k], rl[k], a.x, b.x);
-          df_add_prod(rh[k], rl[k], a.y, b.y);
-          df_add_prod(ih[k], il[k], a.x, b.y);
-          df_add_prod(ih[k], il[k], -a.y, b.x);
-        }
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (c0 + k < ncols) {
-        const double2 s =
-            block_sum2(make_double2((double)rh[k] + (double)rl[k], (double)ih[k] + (double)il[k]), sh);
-        if (threadIdx.x == 0) part[(size_t)(c0 + k) * gridDim.x + blockIdx.x] = s;
-        __syncthreads();
-      }
-    }
-  }
-}
 
 // w = q - a v - b u with a, b split into float pairs (one rounding to FP32)
 __global__ void k_lanczos_w32(float2* w, const float2* q, const float2* __restrict__ v, const float2* __restrict__ u,
@@ -496,6 +462,208 @@ __global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int n
   }
 }
 
+// ---------------------------------------------------------------- complex(8) vectors on the FP32 pipe
+// The same double-float arithmetic for vectors STORED in FP64 (the fast FP64
+// mode and the refinement phase of the complex(4) mode).  A double is split
+// into hi + lo floats with integer instructions only (the FP64 pipe, which
+// also carries double <-> float conversions, would be the bottleneck again):
+// hi keeps the leading 24 significant bits (truncated), lo the next 23, so
+// hi + lo equals the double to 2^-46 relative.  Magnitudes below 2^-80 lose
+// lo, below 2^-126 become 0; such entries are far below the rounding level of
+// a normalised Krylov vector.  Results are widened back to FP64 once per
+// element.
+__device__ __forceinline__ float2 dsplit(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
+  const int e = (int)((h32 >> 20) & 0x7ffu);
+  const unsigned sgn = h32 & 0x80000000u;
+  if (e < 897) return make_float2(0.f, 0.f);
+  if (e > 1150) return make_float2(__uint_as_float(sgn | 0x7f800000u), 0.f);
+  const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+  float lo = 0.f;
+  if (e >= 943) {
+    const unsigned t = (l32 & 0x1fffffffu) >> 6;                               // 23 bits
+    const float f = __fsub_rn(__uint_as_float(0x4b000000u | t), 8388608.0f);  // = t exactly
+    lo = __fmul_rn(f, __uint_as_float(sgn | ((unsigned)(e - 942) << 23)));     // t * 2^(e-1069)
+  }
+  return make_float2(hi, lo);
+}
+__device__ __forceinline__ double djoin(float hi, float lo) { return (double)hi + (double)lo; }
+
+// (hi, lo) += (ah + al) * (bh + bl): exact hi*hi product, cross terms into lo
+__device__ __forceinline__ void df_fma(float& hi, float& lo, float2 a, float2 b) {
+  df_add_prod(hi, lo, a.x, b.x);
+  lo = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, lo));
+}
+__device__ __forceinline__ float2 fneg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+__global__ void __launch_bounds__(kRedThreads) k_dot_part64e(const double2* __restrict__ x,
+                                                             const double2* __restrict__ y, int64_t n,
+                                                             double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x[i], b = y[i];
+    const float2 ar = dsplit(a.x), ai = dsplit(a.y), br = dsplit(b.x), bi = dsplit(b.y);
+    df_fma(rh, rl, ar, br);
+    df_fma(rh, rl, ai, bi);
+    df_fma(ih, il, ar, bi);
+    df_fma(ih, il, fneg2(ai), br);
+  }
+  const double2 s = block_sum2(make_double2(djoin(rh, rl), djoin(ih, il)), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_nrm_part64e(const double2* __restrict__ x, int64_t n,
+                                                             double2* part) {
+  __shared__ double2 sh[kRedThreads];
+  float rh = 0.f, rl = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x[i];
+    const float2 ar = dsplit(a.x), ai = dsplit(a.y);
+    df_fma(rh, rl, ar, ar);
+    df_fma(rh, rl, ai, ai);
+  }
+  const double2 s = block_sum2(make_double2(djoin(rh, rl), 0.0), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+
+// Overlaps conj(V[:, c]) . w for c < ncols.  Grid (column groups of 4,
+// row chunks): block (g, r) accumulates columns 4g..4g+3 over the rows of
+// chunk r (threads stride the chunk), four independent double-float chains
+// per thread at about 40 registers, so many warps hide the load latency.
+// The column groups of one chunk are adjacent in launch order and read the
+// same slice of w, which L2 serves after the first.  Each (column, chunk)
+// partial is a fixed-order block reduction: part[c * nchunk + r].
+template <class T>
+struct SplitLd;
+template <>
+struct SplitLd<double2> {
+  static __device__ __forceinline__ float4 ld(const double2 a) {
+    const float2 r = dsplit(a.x), i = dsplit(a.y);
+    return make_float4(r.x, r.y, i.x, i.y);
+  }
+};
+template <>
+struct SplitLd<float2> {
+  static __device__ __forceinline__ float4 ld(const float2 a) { return make_float4(a.x, 0.f, a.y, 0.f); }
+};
+
+constexpr int kGemvChunks = 304;
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gemv_h3(const T* __restrict__ V, int64_t ldv, int ncols,
+                                                 const T* __restrict__ w, int64_t n, int64_t rows, double2* part) {
+  __shared__ double2 sh[256];
+  const int c0 = 4 * blockIdx.x;
+  const int nc = min(4, ncols - c0);
+  const int64_t r0 = (int64_t)blockIdx.y * rows;
+  const int64_t r1 = min(n, r0 + rows);
+  float acc[4][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
+  for (int64_t i = r0 + threadIdx.x; i < r1; i += 256) {
+    const float4 b = SplitLd<T>::ld(w[i]);
+    const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
+    T a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < nc) a[k] = V[(int64_t)(c0 + k) * ldv + i];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (k < nc) {
+        const float4 av = SplitLd<T>::ld(a[k]);
+        const float2 ar = make_float2(av.x, av.y), ai = make_float2(av.z, av.w);
+        df_fma(acc[k][0], acc[k][1], ar, br);
+        df_fma(acc[k][0], acc[k][1], ai, bi);
+        df_fma(acc[k][2], acc[k][3], ar, bi);
+        df_fma(acc[k][2], acc[k][3], fneg2(ai), br);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (k < nc) {
+      const double2 s = block_sum2(make_double2(djoin(acc[k][0], acc[k][1]), djoin(acc[k][2], acc[k][3])), sh);
+      if (threadIdx.x == 0) part[(size_t)(c0 + k) * gridDim.y + blockIdx.y] = s;
+      __syncthreads();
+    }
+  }
+}
+
+// w -= V[:, :ncols] * coef: the sum over columns in double-float, one FP64
+// subtraction per component at the end
+__global__ void k_gemv_sub64e(const double2* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
+                              double2* __restrict__ w, int64_t n) {
+  __shared__ float4 c[128];  // (re hi, re lo, im hi, im lo)
+  for (int k = threadIdx.x; k < ncols; k += blockDim.x) {
+    const float2 r = dsplit(coef[k].x), m = dsplit(coef[k].y);
+    c[k] = make_float4(r.x, r.y, m.x, m.y);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int k = 0; k < ncols; ++k) {
+      const double2 a = V[(int64_t)k * ldv + i];
+      const float2 ar = dsplit(a.x), ai = dsplit(a.y);
+      const float4 ck = c[k];
+      const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
+      df_fma(rh, rl, cr, ar);
+      df_fma(rh, rl, fneg2(ci), ai);
+      df_fma(ih, il, cr, ai);
+      df_fma(ih, il, ci, ar);
+    }
+    double2 wv = w[i];
+    wv.x -= djoin(rh, rl);
+    wv.y -= djoin(ih, il);
+    w[i] = wv;
+  }
+}
+
+// In-place restart V[:, :nok] = V[:, :nom] * C with split inputs in shared memory.
+__global__ void __launch_bounds__(256) k_restart64e(double2* V, int64_t ldv, int nom, int nok,
+                                                    const double2* __restrict__ C, int64_t n) {
+  extern __shared__ float4 smx[];
+  float4* cs = smx;                          // [nok][nom] split C
+  float4* tile = smx + (size_t)nom * nok;    // [nom][32] split V rows
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  for (int k = threadIdx.x; k < nom * nok; k += blockDim.x) {
+    const float2 r = dsplit(C[k].x), m = dsplit(C[k].y);
+    cs[k] = make_float4(r.x, r.y, m.x, m.y);
+  }
+  for (int k = threadIdx.x; k < nom * 32; k += blockDim.x) {
+    const int col = k / 32, r = k % 32;
+    const int64_t i = r0 + r;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) {
+      const double2 a = V[(int64_t)col * ldv + i];
+      const float2 ar = dsplit(a.x), ai = dsplit(a.y);
+      v = make_float4(ar.x, ar.y, ai.x, ai.y);
+    }
+    tile[k] = v;
+  }
+  __syncthreads();
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t i = r0 + r;
+  if (i < n) {
+    for (int oc = g; oc < nok; oc += 8) {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int j = 0; j < nom; ++j) {
+        const float4 a = tile[j * 32 + r];
+        const float4 c = cs[(size_t)oc * nom + j];
+        const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+        const float2 cr = make_float2(c.x, c.y), ci = make_float2(c.z, c.w);
+        df_fma(rh, rl, ar, cr);
+        df_fma(rh, rl, fneg2(ai), ci);
+        df_fma(ih, il, ar, ci);
+        df_fma(ih, il, ai, cr);
+      }
+      V[(int64_t)oc * ldv + i] = make_double2(djoin(rh, rl), djoin(ih, il));
+    }
+  }
+}
+
 unsigned stream_grid(int64_t n) {
   const int64_t g = (n + 255) / 256;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
@@ -512,6 +680,7 @@ constexpr bool kF32 = std::is_same<T, float2>::value;
 template <class T>
 void Ops<T>::dot(const T* x, const T* y, int64_t n, double2* out) {
   if constexpr (kF32<T>) k_dot_part32<<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
+  else if (eft) k_dot_part64e<<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
   else k_dot_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
   check_launch("k_dot_part");
   k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 0);
@@ -520,6 +689,7 @@ void Ops<T>::dot(const T* x, const T* y, int64_t n, double2* out) {
 template <class T>
 void Ops<T>::nrm(const T* x, int64_t n, double2* out) {
   if constexpr (kF32<T>) k_nrm_part32<<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
+  else if (eft) k_nrm_part64e<<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
   else k_nrm_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, n, part);
   check_launch("k_nrm_part");
   k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 1);
@@ -547,10 +717,17 @@ void Ops<T>::axpy(T* y, const T* x, int64_t n, const double2* a, double sgn) {
 template <class T>
 void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov) {
   if (ncols <= 0) return;
-  if constexpr (kF32<T>) k_gemv_h_part32<<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
-  else k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+  int nb = kRedBlocks;
+  if (kF32<T> || eft) {
+    const int64_t tiles = (n + 255) / 256;
+    nb = (int)std::min<int64_t>(kGemvChunks, tiles);
+    const int64_t rows = (tiles + nb - 1) / nb * 256;
+    k_gemv_h3<T><<<dim3((unsigned)((ncols + 3) / 4), (unsigned)nb), 256, 0, st>>>(V, ldv, ncols, w, n, rows, part);
+  } else {
+    k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+  }
   check_launch("k_gemv_h_part");
-  k_gemv_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, ncols, ov);
+  k_gemv_final<<<ncols, kRedThreads, 0, st>>>(part, nb, ncols, ov);
   check_launch("k_gemv_final");
   gemv_sub(V, ldv, ncols, ov, w, n);
 }
@@ -558,6 +735,7 @@ template <class T>
 void Ops<T>::gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n) {
   if (ncols <= 0) return;
   if constexpr (kF32<T>) k_gemv_sub32<<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  else if (eft) k_gemv_sub64e<<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
   else k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
   check_launch("k_gemv_sub");
 }
@@ -568,6 +746,11 @@ void Ops<T>::restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int6
     if (sm > 48 * 1024)
       QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_restart32<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+  } else if (eft) {
+    const size_t sm = ((size_t)nom * nok + (size_t)nom * 32) * sizeof(float4);
+    if (sm > 48 * 1024)
+      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart64e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_restart64e<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
   } else {
     const size_t sm = ((size_t)nom * 32 + (size_t)nom * nok) * sizeof(double2);
     if (sm > 48 * 1024)
@@ -754,9 +937,9 @@ struct TrlanOut {
 template <class T>
 TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
                     double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes,
-                    double shift = 0.0) {
+                    double shift = 0.0, bool eft = false) {
   const int64_t D = s.D;
-  Ops<T> ops{st, sc.part.get()};
+  Ops<T> ops{st, sc.part.get(), eft};
   double2* alpha = sc.scal;              // [NOM+2]
   double2* beta = sc.scal + (NOM + 2);   // [NOM+2]
   double2* ov = sc.scal + 2 * (NOM + 2); // [NOM+2]
@@ -942,8 +1125,10 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   double tol_est = p.conv_mode == 0 ? p.tol : 0.5 * p.tol;
   TrlanOut r2;
   for (int attempt = 0; attempt < 4; ++attempt) {
+    // precision 1 and 2 refine with double-float arithmetic on the FP32 pipe;
+    // precision 0 keeps FP64 arithmetic throughout
     r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st, sc,
-                             p.reorth_passes);
+                             p.reorth_passes, 0.0, p.precision != 0);
     hv_total += r2.hv_count;
     if (p.conv_mode == 0 || !r2.converged) break;
     Ops<double2> o64{st, sc.part.get()};

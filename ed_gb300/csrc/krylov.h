@@ -21,6 +21,7 @@ template <class T>
 struct Ops {
   cudaStream_t st;
   double2* part;
+  bool eft = false;  // complex(8) only: double-float arithmetic on the FP32 pipe for dots, reorth, restart
   void dot(const T* x, const T* y, int64_t n, double2* out);              // zdotc
   void nrm(const T* x, int64_t n, double2* out);                          // dznrm2 -> out->x
   void scale_inv(T* x, int64_t n, const double2* s);                      // x *= 1/s->x
@@ -64,7 +65,8 @@ void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_b
 struct TrlanParams {
   int NOE = 1, NOK = 2, NOM = 4, maxitr = 1000;
   double tol = 1e-12;
-  int precision = 0;      // 0 complex(8), 1 complex(4) storage + FP64 refinement
+  int precision = 0;      // 0 complex(8) FP64 arithmetic, 1 complex(4) storage + complex(8) refinement,
+                          // 2 complex(8) storage with double-float arithmetic on the FP32 pipe
   int conv_mode = 0;      // 0 reference, 1 residual <= tol, 2 residual <= tol*max(1,|E|)
   uint64_t seed = 1;
   double tol32 = 0.0;     // phase-1 relative residual target (0: default 1e-5)

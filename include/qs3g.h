@@ -113,9 +113,14 @@ int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const in
 /* Thick-restart Lanczos for the lowest NOE eigenpairs.
  * Replaces my_trlanczos_routines_complex + lancz_eigen_val_complex
  * (source/eigen_solver.f90:10-49,69-261; called at source/main.f90:92).
- * precision: 0 = complex(8) Krylov vectors; 1 = complex(4) storage with FP64
- *            reductions, reorthogonalisation and Ritz solve, followed by an FP64
- *            refinement phase.
+ * precision: 0 = complex(8) Krylov vectors and FP64 arithmetic throughout (the
+ *            reference's arithmetic);
+ *            1 = complex(4) storage with FP64-accurate reductions,
+ *            reorthogonalisation and Ritz solve, followed by a complex(8)
+ *            refinement phase run as in precision 2;
+ *            2 = complex(8) storage; dots, reorthogonalisation and restarts in
+ *            double-float arithmetic on the FP32 pipe (about 2^-46 relative
+ *            per operation; GB300 issues FP64 at 1/64 of the FP32 rate).
  * conv_mode: 0 = the reference's test (|E_prev/E - 1| < tol on two consecutive
  *            restarts, eigen_solver.f90:150-159);
  *            1 = Ritz residual |beta_NOM C(NOM,j)| <= tol for j = 1..NOE.

@@ -15,7 +15,9 @@ from ed_gb300 import inputs
 pytestmark = pytest.mark.gpu
 
 
-def _lattice(LX, LY, rng):
+def _lattice(LX, LY):
+    """Square lattice with uniform couplings: the k-sector H is Hermitian
+    only for translation-invariant bonds."""
     bonds = []
     for y in range(LY):
         for x in range(LX):
@@ -23,7 +25,7 @@ def _lattice(LX, LY, rng):
             bonds.append((s, 1 + (x + 1) % LX + LX * y))
             bonds.append((s, 1 + x + LX * ((y + 1) % LY)))
     n = len(bonds)
-    return np.array(bonds, np.int32), rng.uniform(0.5, 1.5, n), rng.uniform(-1, 1, n)
+    return np.array(bonds, np.int32), np.full(n, 1.0), np.full(n, 0.45)
 
 
 CASES = [
@@ -36,7 +38,8 @@ CASES = [
 
 
 def _check_eig(H, ene, psi):
-    w = np.linalg.eigvalsh(H)
+    # zheev('V', 'U') reads the upper triangle
+    w = np.linalg.eigvalsh(H, UPLO="U")
     np.testing.assert_allclose(ene, w, rtol=0, atol=1e-11 * max(1.0, np.abs(w).max()))
     r = H @ psi - psi * ene[None, :]
     assert np.linalg.norm(r, axis=0).max() <= 1e-10 * max(1.0, np.abs(w).max())
@@ -47,11 +50,10 @@ def _check_eig(H, ene, psi):
 def test_full_hamiltonian_and_diag(qs3g, case):
     from ed_gb300 import capi
     NOS, LX, LY, nod, K = case
-    rng = np.random.default_rng(11)
     if LY == 1:
         b, jxy, jz = inputs.chain_bonds(NOS, (1.0, 0.6), (0.3, 0.25))
     else:
-        b, jxy, jz = _lattice(LX, LY, rng)
+        b, jxy, jz = _lattice(LX, LY)
     om = O.Model(NOS, LX, LY, 1, b, jxy, jz, kmax=min(NOS, nod + 2))
     osec = om.build_sector(nod, K)
     h = capi.Handle(NOS, LX, LY, 1, b, jxy, jz)

@@ -165,6 +165,10 @@ def test_trlan_eigenvalues(qs3g, L, nod, K, J1, J2):
     # FP32 storage + FP64 refinement reaches the same eigenvalues
     r32 = h.trlan(NOE, NOK, NOM, maxitr=500, tol=1e-12, precision=1, seed=11)
     np.testing.assert_allclose(r32["ene"], w[:NOE], rtol=1e-10, atol=1e-10)
+    # complex(8) storage with double-float arithmetic on the FP32 pipe
+    re = h.trlan(NOE, NOK, NOM, maxitr=500, tol=1e-12, precision=2, seed=11)
+    np.testing.assert_allclose(re["ene"], w[:NOE], rtol=1e-10, atol=1e-10)
+    assert re["resid"].max() < 1e-8
     # residual-based convergence
     rr = h.trlan(1, 4, 12, maxitr=500, tol=1e-10, conv_mode=1, seed=3)
     assert rr["resid"][0] <= 2e-10
@@ -303,8 +307,10 @@ def test_dsf_all_q_batched(qs3g):
     """Every q of a chain at once (one batched recursion): each q equals the
     oracle's own per-q recursion, and a sweep of one q equals the same q
     inside the full sweep bit for bit (results do not depend on the batch)."""
+    # anisotropic couplings: with SU(2) symmetry S^-(q=0)|GS> is an eigenstate
+    # and the recursion breaks down after one level (beta_2 = 0 up to rounding)
     L, nod = 24, 3
-    b, jxy, jz = inputs.chain_bonds(L, (1.0, 1.0))
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 0.6), (0.2, 0.1))
     om, osec, h, D = both((L, L, 1, 1, b, jxy, jz), nod, (0, 0, 0))
     w, V = np.linalg.eigh(osec.dense())
     psi = np.ascontiguousarray(V[:, 0])
