@@ -284,23 +284,92 @@ def run_gpu(args, rank, world, local_rank, dist):
         line["cpu_baseline"] = {"value": (rows * 48 + nnz_rows * 24) / tc / 1e9, "unit": "GB/s",
                                 "cores": nthreads, "kind": "port",
                                 "sample": f"{rows} rows of {D} timed, extrapolated per byte"}
+    h.close()
     if args.solve and rank == 0:
-        line["gs_solve"] = solve_bench(h, D, args)
+        line["gs_solve"] = solve_bench(args)
+    if args.dsf and rank == 0:
+        line["dsf_batch"] = dsf_bench()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    h.close()
 
 
-def solve_bench(h, D, args):
-    out = {}
-    for name, prec in (("fp64_random", 0), ("fp32store_random", 1)):
+def solve_bench(args):
+    """Ground state of the learned-start workload (L, N_down=4, k=0, Delta=0.7,
+    J2=0.25, an unseen point of the training range) to ||r|| <= tol: plain
+    FP64 TRLan from a random start, complex(4) storage + refinement from a
+    random start, and the same from the network's start vector (trained here
+    on chains L = 48..128 generated by the GPU TRLan itself)."""
+    from ed_gb300 import capi, learned
+    out = {"workload": f"xxz_chain_L{args.L}_Ndown4_k0_Delta0.7_J2_0.25", "tol": args.tol,
+           "NOK": args.nok, "NOM": args.nom}
+    t0 = time.perf_counter()
+    net = capi.Mlp(seed=1)
+    learned.generate(net, learned.training_problems(seed=1))
+    t_gen = time.perf_counter() - t0
+    learned.train(net)
+    out["network"] = {"generate_s": t_gen, "train_s": time.perf_counter() - t0 - t_gen,
+                      "loss": float(net.loss_grad()[0])}
+    h = learned.chain_handle(args.L, 0.7, 0.25)
+    D = h.build_sector(NOD, (0, 0, 0))
+    t0 = time.perf_counter()
+    v = learned.start_vector(net, h, 0.7, 0.25)
+    out["network"]["predict_s"] = time.perf_counter() - t0
+    runs = [("fp32store_learned", 1, v), ("fp32store_random", 1, None), ("fp64_random", 0, None)]
+    psi = None
+    for name, prec, start in runs:
         t0 = time.perf_counter()
-        r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec,
-                    conv_mode=1, seed=7, want_psi=False, allow_unconverged=True)
+        r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec, conv_mode=1,
+                    seed=7, start=start, want_psi=psi is None, allow_unconverged=True)
         dt = time.perf_counter() - t0
+        if psi is None:
+            psi = r["psi"][0]
+            out["learned_start_overlap"] = float(abs(np.vdot(psi, v)) / np.linalg.norm(v))
         out[name] = {"seconds": dt, "hv": r["iters"], "E0": float(r["ene"][0]),
                      "resid": float(r["resid"][0]), "converged": bool(r["converged"])}
+    e64 = out["fp64_random"]["E0"]
+    for name, _, _ in runs:
+        out[name]["dE_vs_fp64"] = abs(out[name]["E0"] - e64)
+    out["speedup_learned_fp32_vs_fp64"] = out["fp64_random"]["seconds"] / out["fp32store_learned"]["seconds"]
+    out["sector_dim"] = D
+    h.close()
     return out
+
+
+def dsf_bench():
+    """All q of a chain at once: L=200 Heisenberg ground state (N_down=3, k=0),
+    S^-(q)|GS> in the N_down=4 sectors for q = 2 pi m / 200, m = 0..199, 150
+    continued-fraction levels each, spectrum on 2000 omega points in [0, 6]
+    with eta = 0.05; the same recursion one q at a time for comparison."""
+    from ed_gb300 import capi, inputs
+    L, nod, itr = 200, 3, 150
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 1.0))
+    h = capi.Handle(L, L, 1, 1, b, jxy, jz)
+    h.build_sector(nod, (0, 0, 0))
+    r = h.trlan(1, 8, 24, maxitr=5000, tol=1e-12, seed=3)
+    psi, e0 = r["psi"][0], float(r["ene"][0])
+    Spos = inputs.chain_positions(L)
+    qs = [(2 * np.pi * m / L, 0.0, 0.0) for m in range(L)]
+    h.dsf(psi, e0, 2, qs[:2], Spos, itr, 0.0)  # warm-up
+    t0 = time.perf_counter()
+    g = h.dsf(psi, e0, 2, qs, Spos, itr, 0.0)
+    t_batch = time.perf_counter() - t0
+    sample = list(range(0, L, 10))
+    t0 = time.perf_counter()
+    same = True
+    for m in sample:
+        one = h.dsf(psi, e0, 2, [qs[m]], Spos, itr, 0.0)
+        same = same and np.array_equal(one["alpha"][0], g["alpha"][m]) and \
+            np.array_equal(one["beta2"][0], g["beta2"][m])
+    t_perq = (time.perf_counter() - t0) * L / len(sample)
+    om = np.linspace(0.0, 6.0, 2000)
+    t0 = time.perf_counter()
+    S = capi.cfrac(g["alpha"], g["beta2"], g["nlev"], g["norm1"], g["E0"], 0.05, om, compat=True)
+    t_cf = time.perf_counter() - t0
+    h.close()
+    return {"workload": "heisenberg_chain_L200_GS_Ndown3_Sminus_all_q_150_levels", "nq": L, "levels": itr,
+            "batched_s": t_batch, "per_q_s_extrapolated": t_perq, "per_q_sample": len(sample),
+            "speedup": t_perq / t_batch, "identical_to_per_q": bool(same), "cfrac_2000_omega_s": t_cf,
+            "spectral_weight_finite": bool(np.isfinite(S[1:]).all())}
 
 
 def main():
@@ -311,11 +380,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--solve", action="store_true")
-    ap.add_argument("--nok", type=int, default=4)
-    ap.add_argument("--nom", type=int, default=24)
-    ap.add_argument("--maxrestart", type=int, default=2000)
-    ap.add_argument("--tol", type=float, default=5e-11)
+    ap.add_argument("--solve", action="store_true",
+                    help="add the ground-state solves (learned start + complex(4) storage vs plain FP64); minutes")
+    ap.add_argument("--dsf", action="store_true", help="add the all-q DSF batch (L=200, 200 q, 150 levels)")
+    ap.add_argument("--nok", type=int, default=16)
+    ap.add_argument("--nom", type=int, default=48)
+    ap.add_argument("--maxrestart", type=int, default=40000)
+    ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--L", type=int, default=1000,
                     help="chain length (1000 is the benchmark; smaller sizes are for profiling)")
     args = ap.parse_args()
