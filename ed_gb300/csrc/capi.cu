@@ -4,9 +4,14 @@
 // a status code plus a message retrievable with qs3g_last_error; nothing
 // throws across the boundary.  Scalars arrive by pointer (Fortran bind(C)
 // by-reference convention).
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <numeric>
+#include <thread>
+#include <vector>
 
 #include "krylov.h"
 #include "mlp.h"
@@ -295,6 +300,62 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
     QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");
     return trlan(h->model, s, p, sm == 1 ? reinterpret_cast<const double2*>(start) : nullptr, ene,
                  reinterpret_cast<double2*>(psi), iters, resid, h->stream);
+  });
+}
+
+int qs3g_trlan_batch(const int* n, qs3g_handle* hs, const int* NOE, const int* NOK, const int* NOM,
+                     const int* maxitr, const double* tol, const int* precision, const int* conv_mode,
+                     const uint64_t* seed, const int* nthreads, double* ene, int* iters, double* resid,
+                     int* status) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(n && hs && NOE && NOK && NOM && maxitr && tol && ene && status, QS3G_EINVAL, "null argument");
+    const int np = *n, noe = *NOE;
+    QS3G_REQUIRE(np >= 0 && noe >= 1, QS3G_EINVAL, "n >= 0 and NOE >= 1");
+    for (int k = 0; k < np; ++k) QS3G_REQUIRE(hs[k] && hs[k]->sector, QS3G_ESTATE, "every handle needs a sector");
+    TrlanParams p;
+    p.NOE = noe; p.NOK = *NOK; p.NOM = *NOM; p.maxitr = *maxitr; p.tol = *tol;
+    p.precision = precision ? *precision : 0;
+    p.conv_mode = conv_mode ? *conv_mode : 0;
+    p.seed = seed ? *seed : 1;
+    QS3G_REQUIRE(p.precision >= 0 && p.precision <= 2, QS3G_EINVAL, "precision must be 0, 1 or 2");
+    // largest sectors first, handed out to the workers from one counter
+    std::vector<int> order(np);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->sector->D > hs[b]->sector->D; });
+    std::atomic<int> next(0);
+    int dev = 0;
+    QS3G_CHECK_CUDA(cudaGetDevice(&dev));
+    auto work = [&]() {
+      cudaSetDevice(dev);
+      for (;;) {
+        const int t = next.fetch_add(1);
+        if (t >= np) break;
+        const int k = order[t];
+        qs3g_ctx* h = hs[k];
+        int it = 0;
+        int rc;
+        try {
+          rc = trlan(h->model, *h->sector, p, nullptr, ene + (size_t)k * noe, nullptr, &it,
+                     resid ? resid + (size_t)k * noe : nullptr, h->stream);
+        } catch (const Error& e) {
+          h->last_error = e.what();
+          rc = e.code;
+        } catch (const std::exception& e) {
+          h->last_error = e.what();
+          rc = QS3G_ECUDA;
+        }
+        if (iters) iters[k] = it;
+        status[k] = rc;
+      }
+    };
+    const int nt = std::max(1, std::min(np, nthreads && *nthreads > 0 ? *nthreads : 8));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    for (int k = 0; k < np; ++k)
+      if (status[k] != QS3G_OK) return (int)status[k];
+    return (int)QS3G_OK;
   });
 }
 

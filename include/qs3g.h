@@ -134,6 +134,20 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
                const int* start_mode, const uint64_t* seed, const qs3g_cplx* start, double* ene,
                qs3g_cplx* psi, int* iters, double* resid);
 
+/* Thick-restart Lanczos on n independent problems at once: hs[0..n-1] are
+ * handles with built sectors (any lattices, sizes and couplings); each is
+ * solved as qs3g_trlan does with a random start, on its own stream, by a pool
+ * of nthreads host workers (NULL or <= 0: 8) taking the largest sectors
+ * first, so the GPU runs the problems' kernels concurrently.  ene (n x NOE),
+ * iters (n, may be NULL), resid (n x NOE, may be NULL) and status (n, the
+ * per-problem return code) are host arrays; the call returns the first
+ * non-OK status.  No counterpart in the reference, which solves one sector
+ * per run (source/main.f90). */
+int qs3g_trlan_batch(const int* n, qs3g_handle* hs, const int* NOE, const int* NOK, const int* NOM,
+                     const int* maxitr, const double* tol, const int* precision, const int* conv_mode,
+                     const uint64_t* seed, const int* nthreads, double* ene, int* iters, double* resid,
+                     int* status);
+
 /* Plain Lanczos (ALG=1) for the lowest eigenpair.
  * Replaces lanczos_routines + lancz_eigen_val (source/lanczos.f90:14-152). */
 int qs3g_lanczos(qs3g_handle h, const int* maxitr, const int* minitr, const int* itrint,
