@@ -35,6 +35,7 @@ EXPORTS = [
     "qs3g_full_hamiltonian", "qs3g_full_diag",
     "qs3g_mlp_create", "qs3g_mlp_destroy", "qs3g_mlp_params", "qs3g_mlp_add_sample", "qs3g_mlp_clear",
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
+    "qs3g_trlan_lockstep",
 ]
 
 MLP_NPARAMS = 35329
@@ -353,6 +354,22 @@ def trlan_batch(handles, NOE, NOK, NOM, maxitr=10000, tol=1e-10, precision=1, co
     rc = load().qs3g_trlan_batch(_i(n), arr, _i(NOE), _i(NOK), _i(NOM), _i(maxitr), _d(tol), _i(precision),
                                  _i(conv_mode), C.byref(C.c_uint64(seed)), _i(nthreads), _ptr(ene), _ptr(iters),
                                  _ptr(resid), _ptr(status))
+    if rc not in (OK, ENOTCONV):
+        _check(rc, None)
+    return ene, iters, resid, status
+
+
+def trlan_lockstep(handles, NOE, NOK, NOM, maxitr=10000, tol=1e-10, precision=1, conv_mode=1, seed=1):
+    """qs3g_trlan_lockstep over chain handles with built sectors: (ene, iters, resid, status)."""
+    n = len(handles)
+    arr = (C.c_void_p * max(1, n))(*[h.h.value if isinstance(h.h, C.c_void_p) else h.h for h in handles])
+    ene = np.zeros((n, NOE))
+    resid = np.zeros((n, NOE))
+    iters = np.zeros(n, np.int32)
+    status = np.zeros(n, np.int32)
+    rc = load().qs3g_trlan_lockstep(_i(n), arr, _i(NOE), _i(NOK), _i(NOM), _i(maxitr), _d(tol), _i(precision),
+                                    _i(conv_mode), C.byref(C.c_uint64(seed)), _ptr(ene), _ptr(iters), _ptr(resid),
+                                    _ptr(status))
     if rc not in (OK, ENOTCONV):
         _check(rc, None)
     return ene, iters, resid, status

@@ -359,6 +359,34 @@ int qs3g_trlan_batch(const int* n, qs3g_handle* hs, const int* NOE, const int* N
   });
 }
 
+int qs3g_trlan_lockstep(const int* n, qs3g_handle* hs, const int* NOE, const int* NOK, const int* NOM,
+                        const int* maxitr, const double* tol, const int* precision, const int* conv_mode,
+                        const uint64_t* seed, double* ene, int* iters, double* resid, int* status) {
+  return guarded(nullptr, [&]() {
+    QS3G_REQUIRE(n && hs && NOE && NOK && NOM && maxitr && tol && ene && status, QS3G_EINVAL, "null argument");
+    const int np = *n;
+    QS3G_REQUIRE(np >= 1, QS3G_EINVAL, "n >= 1");
+    std::vector<const Model*> models(np);
+    std::vector<const Sector*> secs(np);
+    for (int k = 0; k < np; ++k) {
+      QS3G_REQUIRE(hs[k] && hs[k]->sector, QS3G_ESTATE, "every handle needs a sector");
+      models[k] = &hs[k]->model;
+      secs[k] = hs[k]->sector.get();
+    }
+    TrlanParams p;
+    p.NOE = *NOE; p.NOK = *NOK; p.NOM = *NOM; p.maxitr = *maxitr; p.tol = *tol;
+    p.precision = precision ? *precision : 1;
+    p.conv_mode = conv_mode ? *conv_mode : 1;
+    p.seed = seed ? *seed : 1;
+    // every handle's stream may hold its sector build; the batch runs on the first handle's stream
+    for (int k = 0; k < np; ++k) QS3G_CHECK_CUDA(cudaStreamSynchronize(hs[k]->stream));
+    trlan_lockstep(models, secs, p, ene, resid, iters, status, hs[0]->stream);
+    for (int k = 0; k < np; ++k)
+      if (status[k] != QS3G_OK) return (int)status[k];
+    return (int)QS3G_OK;
+  });
+}
+
 int qs3g_lanczos(qs3g_handle h, const int* maxitr, const int* minitr, const int* itrint, const double* tol,
                  const int* start_mode, const uint64_t* seed, const qs3g_cplx* start, double* ene, qs3g_cplx* psi,
                  int* iters) {

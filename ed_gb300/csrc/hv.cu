@@ -166,6 +166,25 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain64_seg(const HvSeg* __re
   else hv_chain_row<NOD, false, double2>(a, xs, ys, g.diag, g.coefR, g.invR, g.chainph, i, shift);
 }
 
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain32_seg(const HvSeg* __restrict__ segs,
+                                                               const int* __restrict__ blk_seg,
+                                                               const int* __restrict__ blk_first,
+                                                               const float2* __restrict__ x,
+                                                               float2* __restrict__ y) {
+  const int sg = blk_seg[blockIdx.x];
+  const HvSeg& g = segs[sg];
+  const int64_t i = (int64_t)(blockIdx.x - blk_first[blockIdx.x]) * blockDim.x + threadIdx.x;
+  if (i >= g.D) return;
+  HvArgs a{};
+  a.D = g.D; a.L = g.L; a.NOS = g.L; a.bits = g.bits;
+  a.conf = g.conf; a.dir = g.dir; a.binomA = g.binomA; a.adj_off = g.adj_off; a.adj = g.adj;
+  const float2* xs = x + g.row0;
+  float2* ys = y + g.row0;
+  if (g.kzero) hv_chain_row<NOD, true, float2>(a, xs, ys, g.diag, g.coefR32, g.invR32, g.chainph32, i, g.shift);
+  else hv_chain_row<NOD, false, float2>(a, xs, ys, g.diag, g.coefR32, g.invR32, g.chainph32, i, g.shift);
+}
+
 // ------------------------------------------------------------ U(1)-only kernels
 // source_only_u1/ham2vec_v3.f90:35-65: no representative search; the hop's
 // row is the colex rank of the flipped configuration (inv_list), computed
@@ -588,7 +607,19 @@ HvSeg make_seg(const Model& m, const Sector& s, int64_t row0) {
   g.conf = s.d_conf.get(); g.dir = s.d_dir.get(); g.binomA = s.d_binomA.get();
   g.adj_off = m.d_adj_off.get(); g.adj = m.d_adj.get();
   g.diag = s.d_diag.get(); g.coefR = s.d_coefR.get(); g.invR = s.d_invR.get(); g.chainph = s.d_chainph.get();
+  g.diag32 = s.d_diag32.get(); g.coefR32 = s.d_coefR32.get(); g.invR32 = s.d_invR32.get();
+  g.chainph32 = s.d_chainph32.get();
+  g.shift = 0.0;
   return g;
+}
+
+void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
+              const float2* x, float2* y, cudaStream_t st) {
+  if (nblk == 0) return;
+  dispatch_nod(NOD, [&](auto c) {
+    k_hv_chain32_seg<decltype(c)::value><<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y);
+  });
+  check_launch("k_hv_chain32_seg");
 }
 
 void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,

@@ -23,6 +23,7 @@
 #include "hosteig.h"
 #include "qs3g_device.cuh"
 #include "qs3g_internal.cuh"
+#include "eft.cuh"
 #include "krylov.h"
 
 namespace qs3g {
@@ -43,19 +44,6 @@ struct Ld<float2> {
   static __device__ __forceinline__ double re(const float2& v) { return (double)v.x; }
   static __device__ __forceinline__ double im(const float2& v) { return (double)v.y; }
 };
-
-__device__ __forceinline__ double2 block_sum2(double2 v, double2* sh) {
-  sh[threadIdx.x] = v;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) {
-      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
-      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
-    }
-    __syncthreads();
-  }
-  return sh[0];
-}
 
 // part[b] = sum over the block's slice of conj(x_i) y_i
 template <class T>
@@ -311,24 +299,6 @@ __global__ void k_residual(double2* __restrict__ w, const double2* __restrict__ 
 //    FP64 for the fixed-order block reduction;
 //  * FP64 scalars (alpha, beta, overlaps, Ritz coefficients) are split into
 //    hi + lo floats, so updates round only once, to the FP32 result.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float p) {
-  const float t = __fadd_rn(hi, p);
-  const float z = __fsub_rn(t, hi);
-  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(p, z));
-  hi = t;
-  lo = __fadd_rn(lo, err);
-}
-__device__ __forceinline__ void df_add_prod(float& hi, float& lo, float a, float b) {
-  const float p = __fmul_rn(a, b);
-  const float e = __fmaf_rn(a, b, -p);
-  df_add(hi, lo, p);
-  lo = __fadd_rn(lo, e);
-}
-__device__ __forceinline__ float2 split(double v) {
-  const float h = (float)v;
-  return make_float2(h, (float)(v - (double)h));
-}
-
 __global__ void __launch_bounds__(kRedThreads) k_dot_part32(const float2* __restrict__ x, const float2* __restrict__ y,
                                                             int64_t n, double2* part) {
   __shared__ double2 sh[kRedThreads];
@@ -472,31 +442,6 @@ __global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int n
 // lo, below 2^-126 become 0; such entries are far below the rounding level of
 // a normalised Krylov vector.  Results are widened back to FP64 once per
 // element.
-__device__ __forceinline__ float2 dsplit(double d) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-  const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
-  const int e = (int)((h32 >> 20) & 0x7ffu);
-  const unsigned sgn = h32 & 0x80000000u;
-  if (e < 897) return make_float2(0.f, 0.f);
-  if (e > 1150) return make_float2(__uint_as_float(sgn | 0x7f800000u), 0.f);
-  const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
-  float lo = 0.f;
-  if (e >= 943) {
-    const unsigned t = (l32 & 0x1fffffffu) >> 6;                               // 23 bits
-    const float f = __fsub_rn(__uint_as_float(0x4b000000u | t), 8388608.0f);  // = t exactly
-    lo = __fmul_rn(f, __uint_as_float(sgn | ((unsigned)(e - 942) << 23)));     // t * 2^(e-1069)
-  }
-  return make_float2(hi, lo);
-}
-__device__ __forceinline__ double djoin(float hi, float lo) { return (double)hi + (double)lo; }
-
-// (hi, lo) += (ah + al) * (bh + bl): exact hi*hi product, cross terms into lo
-__device__ __forceinline__ void df_fma(float& hi, float& lo, float2 a, float2 b) {
-  df_add_prod(hi, lo, a.x, b.x);
-  lo = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, lo));
-}
-__device__ __forceinline__ float2 fneg2(float2 a) { return make_float2(-a.x, -a.y); }
-
 __global__ void __launch_bounds__(kRedThreads) k_dot_part64e(const double2* __restrict__ x,
                                                              const double2* __restrict__ y, int64_t n,
                                                              double2* part) {
@@ -536,20 +481,6 @@ __global__ void __launch_bounds__(kRedThreads) k_nrm_part64e(const double2* __re
 // The column groups of one chunk are adjacent in launch order and read the
 // same slice of w, which L2 serves after the first.  Each (column, chunk)
 // partial is a fixed-order block reduction: part[c * nchunk + r].
-template <class T>
-struct SplitLd;
-template <>
-struct SplitLd<double2> {
-  static __device__ __forceinline__ float4 ld(const double2 a) {
-    const float2 r = dsplit(a.x), i = dsplit(a.y);
-    return make_float4(r.x, r.y, i.x, i.y);
-  }
-};
-template <>
-struct SplitLd<float2> {
-  static __device__ __forceinline__ float4 ld(const float2 a) { return make_float4(a.x, 0.f, a.y, 0.f); }
-};
-
 constexpr int kGemvChunks = 304;
 
 template <class T>
@@ -899,8 +830,6 @@ void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const
 }
 
 // ================================================================ thick-restart Lanczos
-namespace {
-
 // QS3G_VERBOSE=1 prints one progress line per restart, as QS3 does.
 bool verbose() {
   static const bool v = [] {
@@ -909,6 +838,8 @@ bool verbose() {
   }();
   return v;
 }
+
+namespace {
 
 template <class T>
 struct HvOp;

@@ -5,7 +5,10 @@
 
 namespace qs3g {
 
-constexpr int kRedBlocks = 152 * 4;  // fixed reduction grid: 4 blocks per SM of the GB300
+constexpr int kRedBlocks = 152 * 4;
+
+// true when QS3G_VERBOSE is set to a non-zero value (solver progress lines)
+bool verbose();  // fixed reduction grid: 4 blocks per SM of the GB300
 
 // Device scratch of one solve: reduction partials, Lanczos scalars, Ritz coefficients.
 struct Scratch {
@@ -52,6 +55,11 @@ struct HvSeg {
   const double* coefR;
   const double* invR;
   const double2* chainph;
+  const float* diag32;      // complex(4) tables (batched TRLan)
+  const float* coefR32;
+  const float* invR32;
+  const float2* chainph32;
+  double shift;             // per-sector shift of the complex(4) product (H - shift)
 };
 
 HvSeg make_seg(const Model& m, const Sector& s, int64_t row0);
@@ -61,6 +69,10 @@ HvSeg make_seg(const Model& m, const Sector& s, int64_t row0);
 // to whole blocks).
 void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
               const double2* x, double2* y, double shift, cudaStream_t st);
+// complex(4) form: every segment applies H - its own shift
+void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
+              const float2* x, float2* y, cudaStream_t st);
+
 
 struct TrlanParams {
   int NOE = 1, NOK = 2, NOM = 4, maxitr = 1000;
@@ -72,6 +84,11 @@ struct TrlanParams {
   double tol32 = 0.0;     // phase-1 relative residual target (0: default 1e-5)
   int reorth_passes = 1;
 };
+
+// Thick-restart Lanczos on many chain sectors in lock step (batch_trlan.cu).
+// ene, resid: n x NOE; hv: n; status: n (host arrays).
+int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<const Sector*>& secs,
+                   const TrlanParams& p, double* ene, double* resid, int* hv, int* status, cudaStream_t st);
 
 int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
           double2* h_psi, int* iters, double* resid, cudaStream_t st);

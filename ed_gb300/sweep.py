@@ -26,9 +26,12 @@ def random_chains(seed: int = 1, n: int = 256, L_range=(48, 128), nods=(3, 4, 5)
     return out
 
 
-def solve(problems, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, maxitr=20000, nthreads=8, seed=1):
-    """Build every sector, then solve all problems with qs3g_trlan_batch.
-    Returns (records, build seconds, solve seconds)."""
+def solve(problems, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, maxitr=20000, nthreads=8, seed=1,
+          lockstep=False):
+    """Build every sector, then solve all problems with qs3g_trlan_batch
+    (concurrent streams) or, with lockstep=True, qs3g_trlan_lockstep (one
+    launch sequence for all problems).  Returns (records, build seconds,
+    solve seconds)."""
     t0 = time.perf_counter()
     hs = []
     for p in problems:
@@ -37,8 +40,12 @@ def solve(problems, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, maxitr=20000, 
         hs.append(h)
     t_build = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ene, iters, resid, status = capi.trlan_batch(hs, NOE, NOK, NOM, maxitr=maxitr, tol=tol, precision=precision,
-                                                 conv_mode=1, seed=seed, nthreads=nthreads)
+    if lockstep:
+        ene, iters, resid, status = capi.trlan_lockstep(hs, NOE, NOK, NOM, maxitr=maxitr, tol=tol,
+                                                        precision=precision, conv_mode=1, seed=seed)
+    else:
+        ene, iters, resid, status = capi.trlan_batch(hs, NOE, NOK, NOM, maxitr=maxitr, tol=tol, precision=precision,
+                                                     conv_mode=1, seed=seed, nthreads=nthreads)
     t_solve = time.perf_counter() - t0
     recs = []
     for p, h, e, it, r, st in zip(problems, hs, ene, iters, resid, status):

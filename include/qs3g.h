@@ -148,6 +148,19 @@ int qs3g_trlan_batch(const int* n, qs3g_handle* hs, const int* NOE, const int* N
                      const uint64_t* seed, const int* nthreads, double* ene, int* iters, double* resid,
                      int* status);
 
+/* The same n problems solved in lock step: every Krylov column is one
+ * concatenated vector over all problems (chain sectors only), so each
+ * Lanczos step is one launch sequence for all problems, with per-problem
+ * scalars and Ritz solves; converged problems drop out at the next restart.
+ * precision 1 (complex(4) phase + complex(8) refinement, the default) or 2;
+ * conv_mode 1 (default) or 2 verifies every Ritz pair's FP64 residual.  Runs
+ * on the first handle's stream after waiting for every handle's stream.
+ * Arguments and results as qs3g_trlan_batch (no thread count).  No
+ * counterpart in the reference. */
+int qs3g_trlan_lockstep(const int* n, qs3g_handle* hs, const int* NOE, const int* NOK, const int* NOM,
+                        const int* maxitr, const double* tol, const int* precision, const int* conv_mode,
+                        const uint64_t* seed, double* ene, int* iters, double* resid, int* status);
+
 /* Plain Lanczos (ALG=1) for the lowest eigenpair.
  * Replaces lanczos_routines + lancz_eigen_val (source/lanczos.f90:14-152). */
 int qs3g_lanczos(qs3g_handle h, const int* maxitr, const int* minitr, const int* itrint,

@@ -25,3 +25,19 @@ def test_trlan_batch_matches_single_and_dense(qs3g):
         one = h.trlan(2, 4, 12, maxitr=20000, tol=1e-10, precision=1, conv_mode=1, seed=1)
         np.testing.assert_allclose(r["ene"], one["ene"], rtol=0, atol=1e-10)
         h.close()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_trlan_lockstep_matches_dense(qs3g, precision):
+    """All problems in one launch sequence: each problem's two lowest levels
+    equal dense diagonalisation, with FP64 residuals <= 1e-10."""
+    from ed_gb300 import sweep
+    probs = sweep.random_chains(seed=6, n=12, L_range=(14, 22), nods=(3, 4))
+    recs, _, _ = sweep.solve(probs, NOE=2, NOK=4, NOM=12, tol=1e-10, precision=precision, lockstep=True)
+    for p, r in zip(probs, recs):
+        assert r["status"] == 0, r
+        b, jxy, jz = inputs.chain_bonds(p["L"], (1.0, p["delta"]), (p["j2"], p["j2"]))
+        om = O.Model(p["L"], p["L"], 1, 1, b, jxy, jz, kmax=p["nod"] + 2)
+        w = np.linalg.eigvalsh(om.build_sector(p["nod"], (p["K"], 0, 0)).dense())
+        assert abs(r["ene"][0] - w[0]) <= 1e-9 * max(1.0, abs(w[0])), (r["ene"], w[:3])
+        assert max(r["resid"]) <= 1e-10
