@@ -318,12 +318,6 @@ __global__ void __launch_bounds__(kB) k_bresid(const BSeg* segs, const int* bs, 
   w[r] = make_double2(q[r].x - es * v[r].x, q[r].y - es * v[r].y);
 }
 
-template <class T>
-__global__ void k_bconv(T* y, const double2* x, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = T{(decltype(T{}.x))x[i].x, (decltype(T{}.x))x[i].y};
-}
-
 __global__ void k_bto64(double2* y, const float2* x, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = make_double2((double)x[i].x, (double)x[i].y);
