@@ -679,7 +679,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
     QS3G_CHECK_CUDA(cudaMemsetAsync(Q32.get(), 0, ldv * sizeof(float2), st));
     k_bstart<float2><<<all.nblk, kB, 0, st>>>(d_segs.get(), all.d_bs.get(), all.d_bf.get(), V32.get(), p.seed);
     check_launch("k_bstart");
-    const double tol1 = p.tol32 > 0 ? p.tol32 : 1e-6;
+    const double tol1 = phase1_tol(p.tol32);
     lockstep_core<float2>(segs, d_hs, nod_of, on, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, shift,
                           ene, conv, hv, st);
     // phase 2 start: the sum of the NOE Ritz vectors, widened to FP64

@@ -830,6 +830,20 @@ void cfrac_noalloc(int nq, int ldab, const int* nlev, const double* alpha, const
 }
 
 // ================================================================ thick-restart Lanczos
+// Relative residual at which the complex(4) phase of precision 1 hands over
+// to the complex(8) phase: TrlanParams::tol32 when set, else QS3G_TOL32 from
+// the environment, else 1e-6.  The phase also stops when its residual
+// estimate stagnates (the FP32 floor).
+double phase1_tol(double tol32) {
+  if (tol32 > 0) return tol32;
+  static const double v = [] {
+    const char* e = std::getenv("QS3G_TOL32");
+    const double x = e ? std::atof(e) : 0.0;
+    return x > 0 ? x : 1e-6;
+  }();
+  return v;
+}
+
 // QS3G_VERBOSE=1 prints one progress line per restart, as QS3 does.
 bool verbose() {
   static const bool v = [] {
@@ -1028,7 +1042,7 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     Ops<float2> o32{st, sc.part.get()};
     if (start64) o32.from64(V32.get(), start64, D);
     else o32.random_start(V32.get(), D, p.seed);
-    const double tol1 = p.tol32 > 0 ? p.tol32 : 1e-6;
+    const double tol1 = phase1_tol(p.tol32);
     // the complex(4) phase runs on H - sigma, sigma = sum_b Jz_b/4 (the fully polarised energy): the
     // large common diagonal then does not enter the FP32 rounding of H*v
     TrlanOut r1 = trlan_core<float2>(m, s, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, st, sc,

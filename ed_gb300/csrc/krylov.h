@@ -8,7 +8,9 @@ namespace qs3g {
 constexpr int kRedBlocks = 152 * 4;
 
 // true when QS3G_VERBOSE is set to a non-zero value (solver progress lines)
-bool verbose();  // fixed reduction grid: 4 blocks per SM of the GB300
+bool verbose();
+// hand-over residual of the complex(4) phase (see krylov.cu)
+double phase1_tol(double tol32);  // fixed reduction grid: 4 blocks per SM of the GB300
 
 // Device scratch of one solve: reduction partials, Lanczos scalars, Ritz coefficients.
 struct Scratch {
