@@ -35,7 +35,7 @@ EXPORTS = [
     "qs3g_full_hamiltonian", "qs3g_full_diag",
     "qs3g_mlp_create", "qs3g_mlp_destroy", "qs3g_mlp_params", "qs3g_mlp_add_sample", "qs3g_mlp_clear",
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
-    "qs3g_trlan_lockstep",
+    "qs3g_trlan_lockstep", "qs3g_hv_schedule",
 ]
 
 MLP_NPARAMS = 35329
@@ -340,6 +340,17 @@ def _full_diag(h, want_psi=True):
 
 Handle.full_hamiltonian = _full_hamiltonian
 Handle.full_diag = _full_diag
+
+
+def _hv_schedule(h, mode=None):
+    """Set (0 auto, 1 warp per row, 2 thread per row) and/or read the
+    general-lattice H*v schedule of the current sector: (complex(8), complex(4))."""
+    chosen = (C.c_int * 2)()
+    _check(load().qs3g_hv_schedule(h.h, None if mode is None else _i(mode), chosen), h.h)
+    return int(chosen[0]), int(chosen[1])
+
+
+Handle.hv_schedule = _hv_schedule
 
 
 def trlan_batch(handles, NOE, NOK, NOM, maxitr=10000, tol=1e-10, precision=1, conv_mode=1, seed=1,

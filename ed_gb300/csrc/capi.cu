@@ -218,6 +218,21 @@ int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where)
   });
 }
 
+int qs3g_hv_schedule(qs3g_handle h, const int* mode, int* chosen) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    if (mode) {
+      QS3G_REQUIRE(*mode >= 0 && *mode <= 2, QS3G_EINVAL, "schedule must be 0 (auto), 1 (warp) or 2 (thread)");
+      s.hv_schedule64 = s.hv_schedule32 = *mode;
+    }
+    if (chosen) {
+      chosen[0] = s.hv_schedule64;
+      chosen[1] = s.hv_schedule32;
+    }
+    return QS3G_OK;
+  });
+}
+
 int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* where) {
   return guarded(h, [&]() {
     const Sector& s = need_sector(h);

@@ -287,12 +287,18 @@ __device__ __forceinline__ uint64_t general_rep_serial(const int (&o)[NOD], cons
   return best;
 }
 
-// ------------------------------------------------------------ general lattice, complex(8), warp per row
-template <int NOD>
+// ------------------------------------------------------------ general lattice, complex(8)
+// WARP: one warp per row, lanes over the translations, shuffle-min; else one
+// thread per row scanning all translations.  Both visit hops in the same
+// order and break ties the same way (smallest loop index), so they produce
+// identical results; the autotuner below picks the faster per sector.
+template <int NOD, bool WARP>
 __global__ void __launch_bounds__(kHvThreads) k_hv_general64(HvArgs a, const double2* __restrict__ x,
                                                              double2* __restrict__ y) {
-  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int64_t i = WARP ? ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5
+                         : (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = WARP ? (threadIdx.x & 31) : 0;
+  constexpr int kStep = WARP ? 32 : 1;
   if (i >= a.D) return;
   int n[NOD];
   unpack<NOD>(__ldg(a.conf + i), a.bits, n);
@@ -317,17 +323,19 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general64(HvArgs a, const dou
       move_spin<NOD>(n, m, e, o);
       uint64_t best = ~0ull;
       int bt = 0x7fffffff;
-      for (int tau = lane; tau < a.NT; tau += 32) {
+      for (int tau = lane; tau < a.NT; tau += kStep) {
         int ti, tj, tk;
         tau_to_ijk(tau, a, ti, tj, tk);
         const uint64_t v = translate_pack<NOD>(o, ti % a.LX, tj % a.LY, tk % a.LZ, a);
         if (v < best) { best = v; bt = tau; }
       }
+      if constexpr (WARP) {
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
-        if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+        for (int off = 16; off > 0; off >>= 1) {
+          const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
+          if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+        }
       }
       int rep[NOD];
       unpack<NOD>(best, a.bits, rep);
@@ -347,17 +355,19 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general64(HvArgs a, const dou
       acc.y += tv.y;
     }
   }
-  if (lane == 0) {
+  if (lane == 0) {  // thread-per-row: every thread
     const double diag = fma(-2.0, sdown - both, a.Sz_all);
     y[i] = make_double2(fma(diag, xi.x, acc.x), fma(diag, xi.y, acc.y));
   }
 }
 
-template <int NOD>
+template <int NOD, bool WARP>
 __global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const float2* __restrict__ x,
                                                              float2* __restrict__ y, float shift) {
-  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int64_t i = WARP ? ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5
+                         : (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = WARP ? (threadIdx.x & 31) : 0;
+  constexpr int kStep = WARP ? 32 : 1;
   if (i >= a.D) return;
   int n[NOD];
   unpack<NOD>(__ldg(a.conf + i), a.bits, n);
@@ -382,17 +392,19 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_general32(HvArgs a, const flo
       move_spin<NOD>(n, m, e, o);
       uint64_t best = ~0ull;
       int bt = 0x7fffffff;
-      for (int tau = lane; tau < a.NT; tau += 32) {
+      for (int tau = lane; tau < a.NT; tau += kStep) {
         int ti, tj, tk;
         tau_to_ijk(tau, a, ti, tj, tk);
         const uint64_t v = translate_pack<NOD>(o, ti % a.LX, tj % a.LY, tk % a.LZ, a);
         if (v < best) { best = v; bt = tau; }
       }
+      if constexpr (WARP) {
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
-        if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+        for (int off = 16; off > 0; off >>= 1) {
+          const uint64_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int ot = __shfl_xor_sync(0xffffffffu, bt, off);
+          if (ob < best || (ob == best && ot < bt)) { best = ob; bt = ot; }
+        }
       }
       int rep[NOD];
       unpack<NOD>(best, a.bits, rep);
@@ -674,14 +686,48 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
   }
 }
 
+// Schedule of the general-lattice H*v: 1 = warp per row, 2 = thread per row.
+// With the sector's hv_schedule at 0 (auto), the first product of the sector
+// runs both (they give identical results), times them with CUDA events and
+// keeps the faster for every later product of that precision.
+template <class F1, class F2>
+static int autotune(int& slot, F1&& warp, F2&& row, cudaStream_t st) {
+  if (slot != 0) {
+    if (slot == 1) warp(); else row();
+    return slot;
+  }
+  cudaEvent_t e0, e1, e2;
+  QS3G_CHECK_CUDA(cudaEventCreate(&e0));
+  QS3G_CHECK_CUDA(cudaEventCreate(&e1));
+  QS3G_CHECK_CUDA(cudaEventCreate(&e2));
+  QS3G_CHECK_CUDA(cudaEventRecord(e0, st));
+  row();
+  QS3G_CHECK_CUDA(cudaEventRecord(e1, st));
+  warp();
+  QS3G_CHECK_CUDA(cudaEventRecord(e2, st));
+  QS3G_CHECK_CUDA(cudaEventSynchronize(e2));
+  float t_row = 0.f, t_warp = 0.f;
+  QS3G_CHECK_CUDA(cudaEventElapsedTime(&t_row, e0, e1));
+  QS3G_CHECK_CUDA(cudaEventElapsedTime(&t_warp, e1, e2));
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  slot = (t_row < t_warp) ? 2 : 1;
+  return slot;
+}
+
 void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
   if (s.D == 0) return;
   const HvArgs a = make_args(m, s);
-  const unsigned grid = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
-  dispatch_nod(s.NOD, [&](auto c) {
-    k_hv_general64<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y);
-  });
-  check_launch("k_hv_general64");
+  const unsigned gw = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
+  const unsigned gr = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+  auto warp = [&]() {
+    dispatch_nod(s.NOD, [&](auto c) { k_hv_general64<decltype(c)::value, true><<<gw, kHvThreads, 0, st>>>(a, x, y); });
+    check_launch("k_hv_general64");
+  };
+  auto row = [&]() {
+    dispatch_nod(s.NOD, [&](auto c) { k_hv_general64<decltype(c)::value, false><<<gr, kHvThreads, 0, st>>>(a, x, y); });
+    check_launch("k_hv_general64");
+  };
+  autotune(s.hv_schedule64, warp, row, st);
 }
 
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift) {
@@ -701,11 +747,21 @@ void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStrea
     });
     check_launch("k_hv_chain32");
   } else {
-    const unsigned grid = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
-    dispatch_nod(s.NOD, [&](auto c) {
-      k_hv_general32<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
-    });
-    check_launch("k_hv_general32");
+    const unsigned gw = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);
+    const unsigned gr = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
+    auto warp = [&]() {
+      dispatch_nod(s.NOD, [&](auto c) {
+        k_hv_general32<decltype(c)::value, true><<<gw, kHvThreads, 0, st>>>(a, x, y, shift);
+      });
+      check_launch("k_hv_general32");
+    };
+    auto row = [&]() {
+      dispatch_nod(s.NOD, [&](auto c) {
+        k_hv_general32<decltype(c)::value, false><<<gr, kHvThreads, 0, st>>>(a, x, y, shift);
+      });
+      check_launch("k_hv_general32");
+    };
+    autotune(s.hv_schedule32, warp, row, st);
   }
 }
 

@@ -127,6 +127,9 @@ struct Sector {
   DevBuf<float> d_diag32;
   DevBuf<double> d_coefR, d_invR;   // chains: sJxy_b * R[c] and 1/R[c] by self-translation count c
   DevBuf<float> d_coefR32, d_invR32;
+  // general-lattice H*v schedule per precision: 0 = pick on first use,
+  // 1 = warp per row, 2 = thread per row (identical results)
+  mutable int hv_schedule64 = 0, hv_schedule32 = 0;
 };
 
 // Host-side explist (input_param.f90:87-89) and checkstate phases

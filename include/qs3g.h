@@ -94,6 +94,16 @@ int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where)
 /* Same product with complex(4) vectors (FP32 Krylov storage). */
 int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* where);
 
+/* Schedule of the H*v kernel for the current general-lattice sector (chains
+ * and U(1) sectors use one thread per row always): 0 = autotune (the first
+ * product of each precision times a warp per row, lanes over the
+ * translations, against a thread per row scanning them, and keeps the
+ * faster), 1 = warp per row, 2 = thread per row.  Both give identical
+ * results.  mode may be NULL (query only); chosen (may be NULL) receives the
+ * complex(8) and complex(4) schedules (0 until the first product).  No
+ * counterpart in the reference. */
+int qs3g_hv_schedule(qs3g_handle h, const int* mode, int* chosen);
+
 /* The connection table of ham_to_vec_wave_vector: one entry per antiparallel
  * bond whose hop lands on a row of the sector (the `id > 0` branch of
  * source/ham2vec_v3.f90:61-65): 1-based row and column, the translation

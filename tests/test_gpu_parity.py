@@ -330,3 +330,29 @@ def test_dsf_all_q_batched(qs3g):
         np.testing.assert_array_equal(one["alpha"][0], g["alpha"][m])
         np.testing.assert_array_equal(one["beta2"][0], g["beta2"][m])
     h.close()
+
+
+@pytest.mark.parametrize("LX,LY,LZ,nod,K,kind", [(4, 3, 1, 3, (1, 2, 0), "square"), (6, 6, 1, 3, (0, 0, 0), "square")])
+def test_general_hv_schedules_identical(qs3g, LX, LY, LZ, nod, K, kind):
+    """Warp-per-row and thread-per-row general H*v give bit-identical products;
+    the autotuner settles on one of them after the first product."""
+    rng = np.random.default_rng(2)
+    b, jxy, jz = lattice_bonds(LX, LY, LZ, kind, rng)
+    om, osec, h, D = both((LX * LY * LZ, LX, LY, LZ, b, jxy, jz), nod, K)
+    x = rng.standard_normal(D) + 1j * rng.standard_normal(D)
+    x32 = x.astype(np.complex64)
+    out = {}
+    for mode in (1, 2):
+        h.hv_schedule(mode)
+        out[mode] = (h.hv(x), h.hv32(x32))
+        assert h.hv_schedule() == (mode, mode)
+    np.testing.assert_array_equal(out[1][0], out[2][0])
+    np.testing.assert_array_equal(out[1][1], out[2][1])
+    y0 = osec.hv(x)
+    assert np.abs(out[1][0] - y0).max() <= 1e-13 * np.abs(y0).max()
+    h.hv_schedule(0)
+    assert h.hv_schedule() == (0, 0)
+    np.testing.assert_array_equal(h.hv(x), out[1][0])
+    np.testing.assert_array_equal(h.hv32(x32), out[1][1])
+    assert h.hv_schedule()[0] in (1, 2) and h.hv_schedule()[1] in (1, 2)
+    h.close()
