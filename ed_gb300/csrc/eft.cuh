@@ -56,8 +56,10 @@ __device__ __forceinline__ float2 dsplit(double d) {
   const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
   float lo = 0.f;
   if (e >= 943) {
-    const unsigned t = (l32 & 0x1fffffffu) >> 6;                               // 23 bits
-    const float f = __fsub_rn(__uint_as_float(0x4b000000u | t), 8388608.0f);  // = t exactly
+    // the 29 remaining bits rounded to 23 (half up; 2^23 when they carry), so
+    // the split error is unbiased instead of always toward zero
+    const unsigned t = ((l32 & 0x1fffffffu) + 32u) >> 6;
+    const float f = __fsub_rn(__uint_as_float(0x4b000000u | t), 8388608.0f);  // = t exactly (t <= 2^23)
     lo = __fmul_rn(f, __uint_as_float(sgn | ((unsigned)(e - 942) << 23)));     // t * 2^(e-1069)
   }
   return make_float2(hi, lo);

@@ -437,8 +437,8 @@ __global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int n
 // mode and the refinement phase of the complex(4) mode).  A double is split
 // into hi + lo floats with integer instructions only (the FP64 pipe, which
 // also carries double <-> float conversions, would be the bottleneck again):
-// hi keeps the leading 24 significant bits (truncated), lo the next 23, so
-// hi + lo equals the double to 2^-46 relative.  Magnitudes below 2^-80 lose
+// hi keeps the leading 24 significant bits (truncated), lo the remaining 29
+// rounded to 23, so hi + lo equals the double to 2^-47 relative, unbiased.  Magnitudes below 2^-80 lose
 // lo, below 2^-126 become 0; such entries are far below the rounding level of
 // a normalised Krylov vector.  Results are widened back to FP64 once per
 // element.
@@ -1071,9 +1071,26 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   TrlanOut r2;
   for (int attempt = 0; attempt < 4; ++attempt) {
     // precision 1 and 2 refine with double-float arithmetic on the FP32 pipe;
-    // precision 0 keeps FP64 arithmetic throughout
-    r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st, sc,
-                             p.reorth_passes, 0.0, p.precision != 0);
+    // precision 0 keeps FP64 arithmetic throughout.  A continuation (the
+    // recomputed residual missed the target: the double-float floor, about
+    // 1e-12 relative to |E|) runs in FP64 arithmetic.  A breakdown in a
+    // continuation, which starts from a nearly exact eigenvector, keeps the
+    // previous attempt's result (NOE = 1).
+    if (attempt == 0) {
+      r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st,
+                               sc, p.reorth_passes, 0.0, p.precision != 0);
+    } else {
+      try {
+        r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode,
+                                 st, sc, p.reorth_passes, 0.0, false);
+      } catch (const Error& e) {
+        // with NOE = 1 column 0 still holds the (normalised) previous Ritz
+        // vector; with more, the other Ritz vectors were overwritten
+        if (e.code != QS3G_EBREAKDOWN || NOE > 1) throw;
+        if (verbose()) std::printf("trlan: continuation stopped (%s); keeping the previous Ritz pairs\n", e.what());
+        break;
+      }
+    }
     hv_total += r2.hv_count;
     if (p.conv_mode == 0 || !r2.converged) break;
     Ops<double2> o64{st, sc.part.get()};

@@ -129,7 +129,7 @@ int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const in
  *            reorthogonalisation and Ritz solve, followed by a complex(8)
  *            refinement phase run as in precision 2;
  *            2 = complex(8) storage; dots, reorthogonalisation and restarts in
- *            double-float arithmetic on the FP32 pipe (about 2^-46 relative
+ *            double-float arithmetic on the FP32 pipe (about 2^-47 relative
  *            per operation; GB300 issues FP64 at 1/64 of the FP32 rate).
  * conv_mode: 0 = the reference's test (|E_prev/E - 1| < tol on two consecutive
  *            restarts, eigen_solver.f90:150-159);
