@@ -1071,18 +1071,20 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   TrlanOut r2;
   for (int attempt = 0; attempt < 4; ++attempt) {
     // precision 1 and 2 refine with double-float arithmetic on the FP32 pipe;
-    // precision 0 keeps FP64 arithmetic throughout.  A continuation (the
-    // recomputed residual missed the target: the double-float floor, about
-    // 1e-12 relative to |E|) runs in FP64 arithmetic.  A breakdown in a
-    // continuation, which starts from a nearly exact eigenvector, keeps the
-    // previous attempt's result (NOE = 1).
+    // precision 0 keeps FP64 arithmetic throughout.  The first continuation
+    // (the recomputed residual missed the target) stays in double-float; a
+    // second one, at the double-float floor (about 1e-12 relative to |E|),
+    // runs in FP64 arithmetic.  A breakdown in a continuation, which starts
+    // from a nearly exact eigenvector, keeps the previous attempt's result
+    // (NOE = 1).
+    const bool eft = p.precision != 0 && attempt < 2;
     if (attempt == 0) {
       r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st,
-                               sc, p.reorth_passes, 0.0, p.precision != 0);
+                               sc, p.reorth_passes, 0.0, eft);
     } else {
       try {
         r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode,
-                                 st, sc, p.reorth_passes, 0.0, false);
+                                 st, sc, p.reorth_passes, 0.0, eft);
       } catch (const Error& e) {
         // with NOE = 1 column 0 still holds the (normalised) previous Ritz
         // vector; with more, the other Ritz vectors were overwritten
