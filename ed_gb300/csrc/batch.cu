@@ -270,7 +270,6 @@ int dsf_batched(const Model& m, const Sector& gs, const double2* d_psi, double e
       check_launch("k_sscale");
     }
   };
-  int64_t nlaunch = 9 + (int64_t)(itr_dsf - 1) * 6;
   bool captured = false;
   if (st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread) {
     cudaGraph_t graph = nullptr;
@@ -294,7 +293,6 @@ int dsf_batched(const Model& m, const Sector& gs, const double2* d_psi, double e
     }
   }
   if (!captured) record();
-  (void)nlaunch;
   std::vector<double> ha((size_t)nq * ld);
   std::vector<double2> hb((size_t)nq * ld);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(ha.data(), al.get(), ha.size() * 8, cudaMemcpyDeviceToHost, st));

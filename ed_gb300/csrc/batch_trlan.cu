@@ -447,7 +447,6 @@ void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, con
   std::vector<SegState> S(n);
   auto col = [&](int j) { return V + (int64_t)j * ldv; };
   const BSeg* sg = d_segs.get();
-  const bool f32 = sizeof(T) == sizeof(float2);
 
   auto hvop = [&](const T* x, T* y) {
     for (int g = 1; g <= 8; ++g) {
@@ -622,7 +621,6 @@ void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, con
       herm_jacobi(NOM, x.Tm, x.ene, x.Cc);
     }
   }
-  (void)f32;
   for (int s = 0; s < n; ++s) {
     if (S[s].ene.empty()) continue;  // not part of this run
     ene[s].assign(S[s].ene.begin(), S[s].ene.begin() + NOE);

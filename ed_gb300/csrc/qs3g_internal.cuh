@@ -141,9 +141,6 @@ void host_explist(const double rk[3], int LX, int LY, int LZ, std::vector<double
 // ---------------------------------------------------------------- kernels (host wrappers)
 void build_sector(const Model& m, int NOD, const int K[3], Sector& s, cudaStream_t st);
 
-struct HvWork {  // scratch for the general-lattice kernel (none needed today)
-};
-
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
 // complex(4) H*v of H - shift (shift = 0 for the plain product)
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift = 0.f);

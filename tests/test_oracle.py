@@ -233,6 +233,9 @@ NOE = 10, NOK = 15, NOM = 30, maxitr=10000, lnc_ene_conv=1.0d-14, i_vec_min = 1,
     assert q.Ls == (6, 6, 1) and q.K == (0, 0, 0)
     assert q.dynamic["QZ"] == pytest.approx(1.57079632679) and q.dynamic["RFIELD"] == 0.495
     assert q.trlan["LNC_ENE_CONV"] == 1e-14 and q.trlan["NOM"] == 30
+    # a malformed file is refused, not half-read
+    with pytest.raises(ValueError):
+        inputs.read_input("&input_static\nNOV = 2,\n&end\n")
 
 
 def test_bond_file_roundtrip(tmp_path):
