@@ -844,6 +844,19 @@ double phase1_tol(double tol32) {
   return v;
 }
 
+// With a residual target, the first attempt stops when the Ritz estimate
+// |beta_NOM C(NOM, j)| reaches est_factor * tol; the FP64 residual is then
+// recomputed (it can sit above the estimate).  QS3G_EST_FACTOR overrides the
+// default 0.5.
+double est_factor() {
+  static const double v = [] {
+    const char* e = std::getenv("QS3G_EST_FACTOR");
+    const double x = e ? std::atof(e) : 0.0;
+    return (x > 0 && x <= 1) ? x : 0.5;
+  }();
+  return v;
+}
+
 // QS3G_VERBOSE=1 prints one progress line per restart, as QS3 does.
 bool verbose() {
   static const bool v = [] {
@@ -1067,7 +1080,7 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   // below the true residual; the run is accepted only when the FP64 residual
   // ||H psi - E psi|| recomputed from the Ritz vectors meets the target, else it
   // continues from the current Ritz vectors with a tighter estimate target.
-  double tol_est = p.conv_mode == 0 ? p.tol : 0.5 * p.tol;
+  double tol_est = p.conv_mode == 0 ? p.tol : est_factor() * p.tol;
   TrlanOut r2;
   for (int attempt = 0; attempt < 4; ++attempt) {
     // precision 1 and 2 refine with double-float arithmetic on the FP32 pipe;
