@@ -5,14 +5,14 @@
 
 namespace qs3g {
 
-constexpr int kRedBlocks = 152 * 4;
+constexpr int kRedBlocks = 152 * 4;  // fixed reduction grid: 4 blocks per SM of the GB300
 
 // true when QS3G_VERBOSE is set to a non-zero value (solver progress lines)
 bool verbose();
 // hand-over residual of the complex(4) phase (see krylov.cu)
 double phase1_tol(double tol32);
 // first-attempt Ritz-estimate target as a fraction of the residual target
-double est_factor();  // fixed reduction grid: 4 blocks per SM of the GB300
+double est_factor();
 
 // Device scratch of one solve: reduction partials, Lanczos scalars, Ritz coefficients.
 struct Scratch {
