@@ -35,10 +35,11 @@ EXPORTS = [
     "qs3g_full_hamiltonian", "qs3g_full_diag",
     "qs3g_mlp_create", "qs3g_mlp_destroy", "qs3g_mlp_params", "qs3g_mlp_add_sample", "qs3g_mlp_clear",
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
-    "qs3g_trlan_lockstep", "qs3g_hv_schedule",
+    "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real",
 ]
 
 MLP_NPARAMS = 35329
+REAL = 8  # QS3G_REAL: added to a trlan precision for real Krylov vectors
 
 _lib = None
 _lock = threading.Lock()
@@ -186,6 +187,17 @@ class Handle:
         _check(load().qs3g_hv32(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
         return y
 
+    def hv_real(self, x):
+        """y = H x for a real vector x (sectors whose H is real symmetric)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        assert x.shape == (self.D,)
+        y = np.zeros(self.D, np.float64)
+        _check(load().qs3g_hv_real(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
+        return y
+
+    def hv_real_device(self, x_ptr: int, y_ptr: int):
+        _check(load().qs3g_hv_real(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)
+
     def hv32_device(self, x_ptr: int, y_ptr: int):
         _check(load().qs3g_hv32(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)
 
@@ -214,7 +226,10 @@ class Handle:
         return row, col, ell, bond
 
     def trlan(self, NOE, NOK, NOM, maxitr=10000, tol=1e-12, precision=0, conv_mode=0, seed=1,
-              start=None, want_psi=True, allow_unconverged=False):
+              start=None, want_psi=True, allow_unconverged=False, real=False):
+        """qs3g_trlan; real=True adds QS3G_REAL (real Krylov vectors)."""
+        if real:
+            precision |= REAL
         ene = np.zeros(NOE)
         psi = np.zeros((NOE, self.D), np.complex128) if want_psi else None
         resid = np.zeros(NOE)

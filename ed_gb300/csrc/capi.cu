@@ -253,6 +253,27 @@ int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* 
   });
 }
 
+int qs3g_hv_real(qs3g_handle h, double* v0, const double* v1, const int* where) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(v0 && v1 && where, QS3G_EINVAL, "null argument");
+    if (*where == QS3G_DEVICE) {  // asynchronous on the handle's stream
+      hv64r(h->model, s, v1, v0, h->stream, false);
+      return QS3G_OK;
+    }
+    QS3G_REQUIRE(*where == QS3G_HOST, QS3G_EINVAL, "where must be QS3G_HOST or QS3G_DEVICE");
+    QS3G_REQUIRE(real_sector(s), QS3G_ENOTSUP, "real H*v needs a k = 0 chain sector or a U(1) sector");
+    const size_t bytes = (size_t)s.D * sizeof(double);
+    auto* x = static_cast<double*>(staging(h, 0, bytes));
+    auto* y = static_cast<double*>(staging(h, 1, bytes));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(x, v1, bytes, cudaMemcpyHostToDevice, h->stream));
+    hv64r(h->model, s, x, y, h->stream, false);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v0, y, bytes, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
 int qs3g_set_stream(qs3g_handle h, void* stream) {
   return guarded(h, [&]() {
     QS3G_REQUIRE(h, QS3G_EINVAL, "null handle");
@@ -298,6 +319,13 @@ int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const in
   });
 }
 
+// precision 0, 1 or 2, plus QS3G_REAL for real Krylov vectors
+static void set_precision(TrlanParams& p, int v) {
+  p.real = (v & QS3G_REAL) != 0;
+  p.precision = v & ~QS3G_REAL;
+  QS3G_REQUIRE(p.precision >= 0 && p.precision <= 2, QS3G_EINVAL, "precision must be 0, 1 or 2 (+ QS3G_REAL)");
+}
+
 int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, const int* maxitr, const double* tol,
                const int* precision, const int* conv_mode, const int* start_mode, const uint64_t* seed,
                const qs3g_cplx* start, double* ene, qs3g_cplx* psi, int* iters, double* resid) {
@@ -306,10 +334,9 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
     QS3G_REQUIRE(NOE && NOK && NOM && maxitr && tol && ene, QS3G_EINVAL, "null argument");
     TrlanParams p;
     p.NOE = *NOE; p.NOK = *NOK; p.NOM = *NOM; p.maxitr = *maxitr; p.tol = *tol;
-    p.precision = precision ? *precision : 0;
+    set_precision(p, precision ? *precision : 0);
     p.conv_mode = conv_mode ? *conv_mode : 0;
     p.seed = seed ? *seed : 1;
-    QS3G_REQUIRE(p.precision >= 0 && p.precision <= 2, QS3G_EINVAL, "precision must be 0, 1 or 2");
     QS3G_REQUIRE(p.conv_mode >= 0 && p.conv_mode <= 2, QS3G_EINVAL, "conv_mode must be 0, 1 or 2");
     const int sm = start_mode ? *start_mode : 0;
     QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");
@@ -329,10 +356,9 @@ int qs3g_trlan_batch(const int* n, qs3g_handle* hs, const int* NOE, const int* N
     for (int k = 0; k < np; ++k) QS3G_REQUIRE(hs[k] && hs[k]->sector, QS3G_ESTATE, "every handle needs a sector");
     TrlanParams p;
     p.NOE = noe; p.NOK = *NOK; p.NOM = *NOM; p.maxitr = *maxitr; p.tol = *tol;
-    p.precision = precision ? *precision : 0;
+    set_precision(p, precision ? *precision : 0);
     p.conv_mode = conv_mode ? *conv_mode : 0;
     p.seed = seed ? *seed : 1;
-    QS3G_REQUIRE(p.precision >= 0 && p.precision <= 2, QS3G_EINVAL, "precision must be 0, 1 or 2");
     // largest sectors first, handed out to the workers from one counter
     std::vector<int> order(np);
     std::iota(order.begin(), order.end(), 0);

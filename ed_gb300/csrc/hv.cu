@@ -73,25 +73,75 @@ constexpr int kHvThreads = 256;
 // because a chain representative's norm depends only on that count, which
 // chain_rep_count returns with the representative -- so list_r(id) is never
 // gathered.  The 1/list_r(i) factor is applied once per row.
+//
+// V is the vector element: double2 / float2 for complex(8) / complex(4)
+// vectors, double / float for the real vectors of sectors whose H is real
+// symmetric (k = 0 chains, U(1)); P is the complex type of the phase table.
 template <class V>
 struct Cplx;
 template <>
 struct Cplx<double2> {
   using R = double;
+  using P = double2;
   static __device__ __forceinline__ double2 mul(double2 a, double2 b) { return cmul(a, b); }
 };
 template <>
 struct Cplx<float2> {
   using R = float;
+  using P = float2;
   static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return cmulf(a, b); }
 };
+template <>
+struct Cplx<double> {
+  using R = double;
+  using P = double2;
+};
+template <>
+struct Cplx<float> {
+  using R = float;
+  using P = float2;
+};
+
+// one hop: (ax, ay) += c * x(id)
+__device__ __forceinline__ void hop_acc(double c, double2 v, double& ax, double& ay) {
+  ax = fma(c, v.x, ax);
+  ay = fma(c, v.y, ay);
+}
+__device__ __forceinline__ void hop_acc(float c, float2 v, float& ax, float& ay) {
+  ax = fmaf(c, v.x, ax);
+  ay = fmaf(c, v.y, ay);
+}
+__device__ __forceinline__ void hop_acc(double c, double v, double& ax, double&) { ax = fma(c, v, ax); }
+__device__ __forceinline__ void hop_acc(float c, float v, float& ax, float&) { ax = fmaf(c, v, ax); }
+// the row's result di * x(i) + ir * (ax, ay)
+__device__ __forceinline__ double2 row_out(double di, double2 xi, double ir, double ax, double ay) {
+  return make_double2(fma(di, xi.x, ir * ax), fma(di, xi.y, ir * ay));
+}
+__device__ __forceinline__ float2 row_out(float di, float2 xi, float ir, float ax, float ay) {
+  return make_float2(fmaf(di, xi.x, ir * ax), fmaf(di, xi.y, ir * ay));
+}
+__device__ __forceinline__ double row_out(double di, double xi, double ir, double ax, double) {
+  return fma(di, xi, ir * ax);
+}
+__device__ __forceinline__ float row_out(float di, float xi, float ir, float ax, float) {
+  return fmaf(di, xi, ir * ax);
+}
+// the same without a row factor (U(1) rows)
+__device__ __forceinline__ double2 row_out(double di, double2 xi, double ax, double ay) {
+  return make_double2(fma(di, xi.x, ax), fma(di, xi.y, ay));
+}
+__device__ __forceinline__ float2 row_out(float di, float2 xi, float ax, float ay) {
+  return make_float2(fmaf(di, xi.x, ax), fmaf(di, xi.y, ay));
+}
+__device__ __forceinline__ double row_out(double di, double xi, double ax, double) { return fma(di, xi, ax); }
+__device__ __forceinline__ float row_out(float di, float xi, float ax, float) { return fmaf(di, xi, ax); }
 
 template <int NOD, bool KZERO, class V>
 __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
                                              const double* __restrict__ diag,
                                              const typename Cplx<V>::R* __restrict__ coefR,
-                                             const typename Cplx<V>::R* __restrict__ invR, const V* __restrict__ ph,
-                                             int64_t i, double shift) {
+                                             const typename Cplx<V>::R* __restrict__ invR,
+                                             const typename Cplx<V>::P* __restrict__ ph, int64_t i, double shift) {
   using R = typename Cplx<V>::R;
   int n[NOD];
   unpack<NOD>(__ldg(a.conf + i), a.bits, n);
@@ -115,17 +165,12 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
       const int id = dir_lookup32(a.dir, anchored_index32<NOD>(p, a.binomA, a.L));
       if (id < 0) continue;
       V xv = x[id];
-      if (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
-      const R c = __ldg(coefR + (w >> 16) * (NOD + 1) + cnt);
-      ax = fma(c, xv.x, ax);
-      ay = fma(c, xv.y, ay);
+      if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+      hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
     }
   }
   const R ir = __ldg(invR + chain_self_count<NOD>(n, a.L, a.bits));
-  V out;
-  out.x = fma(di, xi.x, ir * ax);
-  out.y = fma(di, xi.y, ir * ay);
-  y[i] = out;
+  y[i] = row_out(di, xi, ir, ax, ay);
 }
 
 template <int NOD, bool KZERO>
@@ -142,6 +187,25 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain32(HvArgs a, const float
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
   hv_chain_row<NOD, KZERO, float2>(a, x, y, a.diag, a.coefR32, a.invR32, a.chainph32, i, (double)shift);
+}
+
+// Real vectors (k = 0): rows 0..D-1; with pad != 0 also a zero in element D
+// (D odd), so that real vectors packed two rows per complex slot keep a zero
+// pad.
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain64r(HvArgs a, const double* __restrict__ x,
+                                                            double* __restrict__ y, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_chain_row<NOD, true, double>(a, x, y, a.diag, a.coefR, a.invR, nullptr, i, 0.0);
+  else if (i == a.D && pad) y[i] = 0.0;
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_chain32r(HvArgs a, const float* __restrict__ x,
+                                                            float* __restrict__ y, float shift, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_chain_row<NOD, true, float>(a, x, y, a.diag, a.coefR32, a.invR32, nullptr, i, (double)shift);
+  else if (i == a.D && pad) y[i] = 0.f;
 }
 
 // ------------------------------------------------------------ batches of chain sectors
@@ -213,16 +277,10 @@ __device__ __forceinline__ void hv_u1_row(const HvArgs& a, const V* __restrict__
       int o[NOD];
       move_spin<NOD>(n, m, e, o);
       const int64_t id = (int64_t)full_index<NOD>(o, a.binom, a.NOS);
-      const V xv = x[id];
-      const R c = __ldg(coefR + (w >> 16) * (NOD + 1));
-      ax = fma(c, xv.x, ax);
-      ay = fma(c, xv.y, ay);
+      hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1)), x[id], ax, ay);
     }
   }
-  V out;
-  out.x = fma(di, xi.x, ax);
-  out.y = fma(di, xi.y, ay);
-  y[i] = out;
+  y[i] = row_out(di, xi, ax, ay);
 }
 
 template <int NOD>
@@ -239,6 +297,22 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_u1_32(HvArgs a, const float2*
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
   hv_u1_row<NOD, float2>(a, x, y, a.coefR32, i, (double)shift);
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_u1_64r(HvArgs a, const double* __restrict__ x,
+                                                          double* __restrict__ y, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_u1_row<NOD, double>(a, x, y, a.coefR, i, 0.0);
+  else if (i == a.D && pad) y[i] = 0.0;
+}
+
+template <int NOD>
+__global__ void __launch_bounds__(kHvThreads) k_hv_u1_32r(HvArgs a, const float* __restrict__ x,
+                                                          float* __restrict__ y, float shift, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_u1_row<NOD, float>(a, x, y, a.coefR32, i, (double)shift);
+  else if (i == a.D && pad) y[i] = 0.f;
 }
 
 // ------------------------------------------------------------ general lattice helpers
@@ -684,6 +758,35 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
   } else {
     hv64_general(m, s, x, y, st);
   }
+}
+
+bool real_sector(const Sector& s) { return s.u1 || (s.anchored && s.kzero); }
+
+// Real vectors of length D; with pad, D odd, also y[D] = 0.
+void hv64r(const Model& m, const Sector& s, const double* x, double* y, cudaStream_t st, bool pad) {
+  QS3G_REQUIRE(real_sector(s), QS3G_ENOTSUP, "real H*v needs a k = 0 chain sector or a U(1) sector");
+  if (s.D == 0) return;
+  const HvArgs a = make_args(m, s);
+  const int pr = (pad && (s.D & 1)) ? 1 : 0;
+  const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
+  dispatch_nod(s.NOD, [&](auto c) {
+    if (s.u1) k_hv_u1_64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+    else k_hv_chain64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+  });
+  check_launch("k_hv_real64");
+}
+
+void hv32r(const Model& m, const Sector& s, const float* x, float* y, cudaStream_t st, float shift, bool pad) {
+  QS3G_REQUIRE(real_sector(s), QS3G_ENOTSUP, "real H*v needs a k = 0 chain sector or a U(1) sector");
+  if (s.D == 0) return;
+  const HvArgs a = make_args(m, s);
+  const int pr = (pad && (s.D & 1)) ? 1 : 0;
+  const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
+  dispatch_nod(s.NOD, [&](auto c) {
+    if (s.u1) k_hv_u1_32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
+    else k_hv_chain32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
+  });
+  check_launch("k_hv_real32");
 }
 
 // Schedule of the general-lattice H*v: 1 = warp per row, 2 = thread per row.

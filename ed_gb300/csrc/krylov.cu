@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 
@@ -174,7 +175,9 @@ __global__ void __launch_bounds__(kRedThreads) k_gemv_h_part(const T* __restrict
 }
 
 // out[c] = sum_b part[c*nb + b]: one block per column, fixed-order tree
-__global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part, int nb, int ncols, double2* out) {
+// (real != 0: the imaginary part is dropped)
+__global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part, int nb, int ncols, double2* out,
+                                                            int real) {
   __shared__ double2 sh[kRedThreads];
   const int c = blockIdx.x;
   double2 acc = make_double2(0.0, 0.0);
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part,
     acc.y += part[(size_t)c * nb + i].y;
   }
   const double2 s = block_sum2(acc, sh);
-  if (threadIdx.x == 0) out[c] = s;
+  if (threadIdx.x == 0) out[c] = real ? make_double2(s.x, 0.0) : s;
 }
 
 // w -= V[:, :ncols] * coef   (coef from device memory)
@@ -282,8 +285,8 @@ __global__ void k_random_start(T* x, int64_t n, uint64_t seed) {
 }
 
 // w = q - e * v  (residual), FP64
-__global__ void k_residual(double2* __restrict__ w, const double2* __restrict__ q, const double2* __restrict__ v,
-                           int64_t n, double e) {
+// w = q - e v (w may be q)
+__global__ void k_residual(double2* w, const double2* q, const double2* __restrict__ v, int64_t n, double e) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     w[i] = make_double2(q[i].x - e * v[i].x, q[i].y - e * v[i].y);
 }
@@ -595,6 +598,18 @@ __global__ void __launch_bounds__(256) k_restart64e(double2* V, int64_t ldv, int
   }
 }
 
+// Real vectors two rows per complex slot: out[r] = Re in[r] for r < D, and a
+// zero pad when D is odd; unpack writes (x[r], 0).
+__global__ void k_pack_real(double* __restrict__ out, const double2* __restrict__ in, int64_t D) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D + (D & 1);
+       r += (int64_t)gridDim.x * blockDim.x)
+    out[r] = r < D ? in[r].x : 0.0;
+}
+__global__ void k_unpack_real(double2* __restrict__ out, const double* __restrict__ in, int64_t D) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < D; r += (int64_t)gridDim.x * blockDim.x)
+    out[r] = make_double2(in[r], 0.0);
+}
+
 unsigned stream_grid(int64_t n) {
   const int64_t g = (n + 255) / 256;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
@@ -614,7 +629,7 @@ void Ops<T>::dot(const T* x, const T* y, int64_t n, double2* out) {
   else if (eft) k_dot_part64e<<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
   else k_dot_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, y, n, part);
   check_launch("k_dot_part");
-  k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, 0);
+  k_red_final<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, out, real ? 2 : 0);
   check_launch("k_red_final");
 }
 template <class T>
@@ -635,8 +650,9 @@ void Ops<T>::scale_inv(T* x, int64_t n, const double2* s) {
 template <class T>
 void Ops<T>::lanczos_w(T* w, const T* q, const T* v, const T* u, int64_t n, const double2* a, const double2* b,
                        bool real_alpha) {
-  if constexpr (kF32<T>) k_lanczos_w32<<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
-  else k_lanczos_w<T><<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, real_alpha ? 1 : 0);
+  const int ra = (real_alpha || real) ? 1 : 0;
+  if constexpr (kF32<T>) k_lanczos_w32<<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, ra);
+  else k_lanczos_w<T><<<stream_grid(n), 256, 0, st>>>(w, q, v, u, n, a, b, ra);
   check_launch("k_lanczos_w");
 }
 template <class T>
@@ -658,7 +674,7 @@ void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2
     k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
   }
   check_launch("k_gemv_h_part");
-  k_gemv_final<<<ncols, kRedThreads, 0, st>>>(part, nb, ncols, ov);
+  k_gemv_final<<<ncols, kRedThreads, 0, st>>>(part, nb, ncols, ov, real ? 1 : 0);
   check_launch("k_gemv_final");
   gemv_sub(V, ldv, ncols, ov, w, n);
 }
@@ -872,14 +888,18 @@ template <class T>
 struct HvOp;
 template <>
 struct HvOp<double2> {
-  static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st, double) {
-    hv64(m, s, x, y, st);
+  static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st, double,
+                    bool real) {
+    if (real) hv64r(m, s, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), st, true);
+    else hv64(m, s, x, y, st);
   }
 };
 template <>
 struct HvOp<float2> {
-  static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, double shift) {
-    hv32(m, s, x, y, st, (float)shift);
+  static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, double shift,
+                    bool real) {
+    if (real) hv32r(m, s, reinterpret_cast<const float*>(x), reinterpret_cast<float*>(y), st, (float)shift, true);
+    else hv32(m, s, x, y, st, (float)shift);
   }
 };
 
@@ -890,14 +910,24 @@ struct TrlanOut {
   int restarts = 0;
 };
 
+// FP64 residual of the Ritz pairs in V[:, :NOE] with Ritz values ene[0..NOE):
+// the largest, in the units of conv_mode.
+using RitzCheck = std::function<double(const std::vector<double>& ene)>;
+
 // lancz_eigen_val_complex (eigen_solver.f90:69-261) on device vectors of type T.
 // V must hold NOM+1 columns of length ldv; V[:,0] holds the start vector.
+// real: the vectors are real, two rows per T slot (real_sector(s)); every
+// scalar of the recurrence (alpha, overlaps, Ritz coefficients) is then real.
+// check (conv_mode 1, 2): once the Ritz estimate is within 4x of target, each
+// restart also recomputes the true residual and stops as soon as it meets
+// target -- an early exit only; the iteration itself is unchanged.
 template <class T>
 TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
                     double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes,
-                    double shift = 0.0, bool eft = false) {
-  const int64_t D = s.D;
-  Ops<T> ops{st, sc.part.get(), eft};
+                    double shift = 0.0, bool eft = false, bool real = false, const RitzCheck& check = RitzCheck(),
+                    double target = 0.0) {
+  const int64_t D = real ? (s.D + 1) / 2 : s.D;  // T slots per vector
+  Ops<T> ops{st, sc.part.get(), eft, real};
   double2* alpha = sc.scal;              // [NOM+2]
   double2* beta = sc.scal + (NOM + 2);   // [NOM+2]
   double2* ov = sc.scal + 2 * (NOM + 2); // [NOM+2]
@@ -912,7 +942,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
   ops.nrm(col(0), D, beta + 0);
   for (int i = 1; i <= NOM; ++i) {
     ops.scale_inv(col(i - 1), D, beta + (i - 1));
-    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     if (i > 1) {
@@ -947,7 +977,8 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
   for (int tritr = 1; tritr <= maxitr; ++tritr) {
     out.restarts = tritr;
     for (int j = 0; j < NOK; ++j)
-      for (int i = 0; i < NOM; ++i) hC[(size_t)j * NOM + i] = make_double2(Cc[i + (size_t)j * NOM].real(), Cc[i + (size_t)j * NOM].imag());
+      for (int i = 0; i < NOM; ++i)
+        hC[(size_t)j * NOM + i] = make_double2(Cc[i + (size_t)j * NOM].real(), real ? 0.0 : Cc[i + (size_t)j * NOM].imag());
     QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, hC.data(), hC.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
     ops.restart(V, ldv, NOM, NOK, sc.C, D);
     // convergence (eigen_solver.f90:150-159) or the Ritz residual bound
@@ -964,8 +995,16 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     flag = (max_conv < tol) ? flag + 1 : 0;
     if (verbose())  // the progress line of eigen_solver.f90:157-158
       std::printf("tritr, ene(NOK), max_conv, flag: %5d %25.15e %11.1e %5d  (%s, hv=%d)\n", tritr, ene[NOK - 1],
-                  max_conv, flag, sizeof(T) == 8 ? "complex(4)" : "complex(8)", out.hv_count);
-    if ((conv_mode == 0 && flag == 2) || (conv_mode != 0 && flag >= 1)) {
+                  max_conv, flag, sizeof(T) == 8 ? "complex(4)" : (ops.eft ? "complex(8) df" : "complex(8) fp64"),
+                  out.hv_count);
+    bool done = (conv_mode == 0 && flag == 2) || (conv_mode != 0 && flag >= 1);
+    if (!done && check && max_conv < 4.0 * target) {
+      const double worst = check(ene);
+      out.hv_count += NOE;
+      if (verbose()) std::printf("trlan: residual check at estimate %.2e: %.3e\n", max_conv, worst);
+      done = worst <= target;
+    }
+    if (done) {
       out.converged = true;
       break;
     }
@@ -978,10 +1017,10 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     for (int j = 0; j < NOK; ++j) calpha[j + 1] = ene[j];
     for (int j = 1; j <= NOK; ++j) cbeta[j] = cbeta[NOM] * Cc[(NOM - 1) + (size_t)(j - 1) * NOM];
     std::vector<double2> hcb(NOK);
-    for (int j = 0; j < NOK; ++j) hcb[j] = make_double2(cbeta[j + 1].real(), cbeta[j + 1].imag());
+    for (int j = 0; j < NOK; ++j) hcb[j] = make_double2(cbeta[j + 1].real(), real ? 0.0 : cbeta[j + 1].imag());
     QS3G_CHECK_CUDA(cudaMemcpyAsync(cb, hcb.data(), NOK * sizeof(double2), cudaMemcpyHostToDevice, st));
     int i = NOK + 1;
-    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     ops.gemv_sub(V, ldv, NOK, cb, Q, D);
@@ -990,7 +1029,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     ops.nrm(col(i), D, beta + i);
     for (i = NOK + 2; i <= NOM; ++i) {
       ops.scale_inv(col(i - 1), D, beta + (i - 1));
-      HvOp<T>::apply(m, s, col(i - 1), Q, st, shift);
+      HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
       ++out.hv_count;
       ops.dot(col(i - 1), Q, D, alpha + i);
       ops.lanczos_w(col(i), Q, col(i - 1), col(i - 2), D, alpha + i, beta + (i - 1), false);
@@ -1002,7 +1041,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     QS3G_CHECK_CUDA(cudaMemcpyAsync(hb.data(), beta, (NOM + 2) * sizeof(double2), cudaMemcpyDeviceToHost, st));
     QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
     for (int j = NOK + 1; j <= NOM; ++j) {
-      calpha[j] = zd(ha[j].x, ha[j].y);
+      calpha[j] = zd(ha[j].x, real ? 0.0 : ha[j].y);
       cbeta[j] = hb[j].x;
       QS3G_REQUIRE(std::isfinite(hb[j].x) && hb[j].x > 0.0 && std::isfinite(ha[j].x), QS3G_EBREAKDOWN,
                    "Lanczos breakdown after a restart");
@@ -1035,69 +1074,108 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   const int64_t D = s.D;
   QS3G_REQUIRE(D >= NOE && D >= NOK && D >= NOM, QS3G_EINVAL, "sector dimension smaller than NOM (stop 999)");
   QS3G_REQUIRE(NOM <= 120, QS3G_EINVAL, "NOM must be <= 120");
-  const int64_t ldv = (D + 31) / 32 * 32;
+  const bool real = p.real;
+  QS3G_REQUIRE(!real || real_sector(s), QS3G_ENOTSUP, "real arithmetic needs a k = 0 chain sector or a U(1) sector");
+  // complex slots per Krylov vector: D, or ceil(D/2) for real vectors (two
+  // rows per slot, a zero pad row when D is odd)
+  const int64_t n = real ? (D + 1) / 2 : D;
+  const int64_t ldv = (n + 31) / 32 * 32;
+  auto hv_fp64 = [&](const double2* x, double2* y) {
+    if (real) hv64r(m, s, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), st, true);
+    else hv64(m, s, x, y, st);
+  };
   Scratch sc;
   sc.ensure(NOM);
   int hv_total = 0;
   std::vector<double> ene;
-  DevBuf<double2> d_start;
+  DevBuf<double2> d_start, d_pack;
   const double2* start64 = nullptr;
   if (h_start) {
     d_start.alloc(D);
     QS3G_CHECK_CUDA(cudaMemcpyAsync(d_start.get(), h_start, D * sizeof(double2), cudaMemcpyHostToDevice, st));
     start64 = d_start.get();
+    if (real) {  // the real part of the given start vector
+      d_pack.alloc(n);
+      k_pack_real<<<stream_grid(n), 256, 0, st>>>(reinterpret_cast<double*>(d_pack.get()), start64, D);
+      check_launch("k_pack_real");
+      start64 = d_pack.get();
+    }
   }
   bool converged = false;
   DevBuf<double2> V64((size_t)ldv * (NOM + 1)), Q64(D);
   if (p.precision == 1) {
     // phase 1: complex(4) Krylov storage, FP64 reductions and Ritz solve
-    DevBuf<float2> V32((size_t)ldv * (NOM + 1)), Q32(D);
+    DevBuf<float2> V32((size_t)ldv * (NOM + 1)), Q32(n);
     Ops<float2> o32{st, sc.part.get()};
-    if (start64) o32.from64(V32.get(), start64, D);
-    else o32.random_start(V32.get(), D, p.seed);
+    if (start64) o32.from64(V32.get(), start64, n);
+    else o32.random_start(V32.get(), n, p.seed);
+    if (real && (D & 1)) QS3G_CHECK_CUDA(cudaMemsetAsync(reinterpret_cast<float*>(V32.get()) + D, 0, sizeof(float), st));
     const double tol1 = phase1_tol(p.tol32);
     // the complex(4) phase runs on H - sigma, sigma = sum_b Jz_b/4 (the fully polarised energy): the
     // large common diagonal then does not enter the FP32 rounding of H*v
     TrlanOut r1 = trlan_core<float2>(m, s, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, st, sc,
-                                     p.reorth_passes, m.Sz_all);
+                                     p.reorth_passes, m.Sz_all, false, real);
     hv_total += r1.hv_count;
     // phase 2: FP64 thick-restart Lanczos from the sum of the NOE Ritz vectors
     Ops<double2> o64{st, sc.part.get()};
-    f32_to_f64(V64.get(), V32.get(), D, st);
+    f32_to_f64(V64.get(), V32.get(), n, st);
     for (int j = 1; j < NOE; ++j) {
-      f32_to_f64(Q64.get(), V32.get() + (int64_t)j * ldv, D, st);
+      f32_to_f64(Q64.get(), V32.get() + (int64_t)j * ldv, n, st);
       std::vector<double2> one(1, make_double2(1.0, 0.0));
       QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, one.data(), sizeof(double2), cudaMemcpyHostToDevice, st));
-      o64.axpy(V64.get(), Q64.get(), D, sc.C, 1.0);
+      o64.axpy(V64.get(), Q64.get(), n, sc.C, 1.0);
     }
   } else {
     Ops<double2> o64{st, sc.part.get()};
-    if (start64) QS3G_CHECK_CUDA(cudaMemcpyAsync(V64.get(), start64, D * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    else o64.random_start(V64.get(), D, p.seed);
+    if (start64) QS3G_CHECK_CUDA(cudaMemcpyAsync(V64.get(), start64, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    else o64.random_start(V64.get(), n, p.seed);
+    if (real && (D & 1)) QS3G_CHECK_CUDA(cudaMemsetAsync(reinterpret_cast<double*>(V64.get()) + D, 0, sizeof(double), st));
   }
   const int hv_phase1 = hv_total;
   // With a residual target (conv_mode 1, 2) the Ritz estimate |beta C| can sit
   // below the true residual; the run is accepted only when the FP64 residual
   // ||H psi - E psi|| recomputed from the Ritz vectors meets the target, else it
-  // continues from the current Ritz vectors with a tighter estimate target.
+  // continues from the Ritz vectors (a fresh Lanczos start: continuing the
+  // same thick restart would keep the orthogonality its basis has lost against
+  // the converged vector, which at L = 400 held the residual at 1.2e-10) with
+  // a tighter estimate target.
   double tol_est = p.conv_mode == 0 ? p.tol : est_factor() * p.tol;
+  // Precision 1 and 2 refine with double-float arithmetic on the FP32 pipe
+  // and precision 0 in FP64.  The first continuation stays in double-float;
+  // from the second on (at the double-float floor, about 1e-12 relative to
+  // |E|) they run in FP64 arithmetic.  Every attempt stops early when the
+  // recomputed residual meets the target (trlan_core's check).  A breakdown
+  // in a continuation, which starts from a nearly exact eigenvector, keeps
+  // the previous attempt's result (NOE = 1).
+  RitzCheck check;
+  if (p.conv_mode != 0) {
+    check = [&](const std::vector<double>& e) {
+      Ops<double2> o64{st, sc.part.get()};
+      double worst = 0.0;
+      for (int j = 0; j < NOE; ++j) {
+        double2* pj = V64.get() + (int64_t)j * ldv;
+        hv_fp64(pj, Q64.get());
+        residual64(Q64.get(), Q64.get(), pj, n, e[j], st);
+        o64.nrm(Q64.get(), n, sc.scal);  // sc.scal[0] = alpha[0], never used
+        double2 rr;
+        QS3G_CHECK_CUDA(cudaMemcpyAsync(&rr, sc.scal, sizeof(double2), cudaMemcpyDeviceToHost, st));
+        QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+        const double scale = p.conv_mode == 2 ? std::max(1.0, std::fabs(e[j])) : 1.0;
+        worst = std::max(worst, rr.x / scale);
+      }
+      return worst;
+    };
+  }
   TrlanOut r2;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    // precision 1 and 2 refine with double-float arithmetic on the FP32 pipe;
-    // precision 0 keeps FP64 arithmetic throughout.  The first continuation
-    // (the recomputed residual missed the target) stays in double-float; a
-    // second one, at the double-float floor (about 1e-12 relative to |E|),
-    // runs in FP64 arithmetic.  A breakdown in a continuation, which starts
-    // from a nearly exact eigenvector, keeps the previous attempt's result
-    // (NOE = 1).
     const bool eft = p.precision != 0 && attempt < 2;
     if (attempt == 0) {
       r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st,
-                               sc, p.reorth_passes, 0.0, eft);
+                               sc, p.reorth_passes, 0.0, eft, real, check, p.tol);
     } else {
       try {
         r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode,
-                                 st, sc, p.reorth_passes, 0.0, eft);
+                                 st, sc, p.reorth_passes, 0.0, eft, real, check, p.tol);
       } catch (const Error& e) {
         // with NOE = 1 column 0 still holds the (normalised) previous Ritz
         // vector; with more, the other Ritz vectors were overwritten
@@ -1109,13 +1187,12 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     hv_total += r2.hv_count;
     if (p.conv_mode == 0 || !r2.converged) break;
     Ops<double2> o64{st, sc.part.get()};
-    DevBuf<double2> W(D);
     double worst = 0.0;
     for (int j = 0; j < NOE; ++j) {
       double2* pj = V64.get() + (int64_t)j * ldv;
-      hv64(m, s, pj, Q64.get(), st);
-      residual64(W.get(), Q64.get(), pj, D, r2.ene[j], st);
-      o64.nrm(W.get(), D, sc.scal);
+      hv_fp64(pj, Q64.get());
+      residual64(Q64.get(), Q64.get(), pj, n, r2.ene[j], st);
+      o64.nrm(Q64.get(), n, sc.scal);
       double2 rr;
       QS3G_CHECK_CUDA(cudaMemcpyAsync(&rr, sc.scal, sizeof(double2), cudaMemcpyDeviceToHost, st));
       QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -1131,7 +1208,7 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     for (int j = 1; j < NOE; ++j) {
       std::vector<double2> one(1, make_double2(1.0, 0.0));
       QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C, one.data(), sizeof(double2), cudaMemcpyHostToDevice, st));
-      o64.axpy(V64.get(), V64.get() + (int64_t)j * ldv, D, sc.C, 1.0);
+      o64.axpy(V64.get(), V64.get() + (int64_t)j * ldv, n, sc.C, 1.0);
     }
   }
   if (verbose()) std::printf("trlan: %d H*v in the complex(4) phase, %d in the complex(8) phase\n", hv_phase1,
@@ -1147,16 +1224,23 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     for (int j = 0; j < NOE; ++j) {
       double2* pj = V64.get() + (int64_t)j * ldv;
       if (resid) {
-        hv64(m, s, pj, Q64.get(), st);
-        residual64(W.get(), Q64.get(), pj, D, ene[j], st);
-        o64.nrm(W.get(), D, sc.scal);
+        hv_fp64(pj, Q64.get());
+        residual64(W.get(), Q64.get(), pj, n, ene[j], st);
+        o64.nrm(W.get(), n, sc.scal);
         double2 r;
         QS3G_CHECK_CUDA(cudaMemcpyAsync(&r, sc.scal, sizeof(double2), cudaMemcpyDeviceToHost, st));
         QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
         resid[j] = r.x;
       }
-      if (h_psi)
-        QS3G_CHECK_CUDA(cudaMemcpyAsync(h_psi + (int64_t)j * D, pj, D * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      if (h_psi) {
+        const double2* src = pj;
+        if (real) {  // (psi_r, 0)
+          k_unpack_real<<<stream_grid(D), 256, 0, st>>>(W.get(), reinterpret_cast<const double*>(pj), D);
+          check_launch("k_unpack_real");
+          src = W.get();
+        }
+        QS3G_CHECK_CUDA(cudaMemcpyAsync(h_psi + (int64_t)j * D, src, D * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      }
     }
     QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
   }

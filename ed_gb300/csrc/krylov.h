@@ -29,6 +29,9 @@ struct Ops {
   cudaStream_t st;
   double2* part;
   bool eft = false;  // complex(8) only: double-float arithmetic on the FP32 pipe for dots, reorth, restart
+  // Real vectors stored two rows per complex slot (sectors with a real
+  // symmetric H): dots and overlaps keep their real parts, alpha is real.
+  bool real = false;
   void dot(const T* x, const T* y, int64_t n, double2* out);              // zdotc
   void nrm(const T* x, int64_t n, double2* out);                          // dznrm2 -> out->x
   void scale_inv(T* x, int64_t n, const double2* s);                      // x *= 1/s->x
@@ -87,6 +90,7 @@ struct TrlanParams {
   uint64_t seed = 1;
   double tol32 = 0.0;     // phase-1 relative residual target (0: default 1e-5)
   int reorth_passes = 1;
+  bool real = false;      // real Krylov vectors (real_sector(s) only)
 };
 
 // Thick-restart Lanczos on many chain sectors in lock step (batch_trlan.cu).

@@ -145,6 +145,13 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
 // complex(4) H*v of H - shift (shift = 0 for the plain product)
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift = 0.f);
 void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+// Sectors whose H is real symmetric: chains at k = 0 and U(1) sectors.  For
+// them hv64r / hv32r multiply real vectors x, y of length D; with pad and D
+// odd they also write y[D] = 0, the pad of a real vector stored two rows per
+// complex slot.  Other sectors: QS3G_ENOTSUP.
+bool real_sector(const Sector& s);
+void hv64r(const Model& m, const Sector& s, const double* x, double* y, cudaStream_t st, bool pad);
+void hv32r(const Model& m, const Sector& s, const float* x, float* y, cudaStream_t st, float shift, bool pad);
 
 // dense H(i, id) of make_full_hamiltonian, column-major with leading dimension ld
 // (zeroed here), accumulated in the reference's bond order

@@ -8,6 +8,8 @@ module qs3g_iface
   implicit none
 
   integer(c_int), parameter :: QS3G_OK = 0, QS3G_HOST = 0, QS3G_DEVICE = 1
+  ! added to qs3g_trlan's precision: real Krylov vectors (k = 0 chains, U(1))
+  integer(c_int), parameter :: QS3G_REAL = 8
 
   interface
     ! state set up by read_ip / get_combination / mk_shift_*_SQ
@@ -44,6 +46,14 @@ module qs3g_iface
       import :: c_ptr, c_int, c_double_complex
       type(c_ptr), value :: h
       complex(c_double_complex) :: v0(*), v1(*)
+      integer(c_int) :: where
+    end function
+
+    ! the same product on real vectors (sectors with a real symmetric H)
+    integer(c_int) function qs3g_hv_real(h, v0, v1, where) bind(C, name="qs3g_hv_real")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: v0(*), v1(*)
       integer(c_int) :: where
     end function
 

@@ -41,6 +41,17 @@ enum {
 /* Location of vector arguments. */
 enum { QS3G_HOST = 0, QS3G_DEVICE = 1 };
 
+/* Added to qs3g_trlan's precision (0, 1, 2): real Krylov vectors for sectors
+ * whose H is real symmetric (chains at k = 0, U(1) sectors), stored two rows
+ * per complex slot, with every scalar of the recurrence real -- half the bytes
+ * of each vector pass and one FP64 FMA per hop in H*v.  The start vector is
+ * the real part of the given one (or a real random vector); psi is returned
+ * with zero imaginary parts.  A real start vector has one component in each
+ * eigenspace, so a degenerate eigenvalue is found once (a complex start finds
+ * its other copies only through rounding); for more than one eigenpair of a
+ * sector with degeneracies use the complex modes. */
+enum { QS3G_REAL = 8 };
+
 /* Create a handle for the lattice and bonds.
  * Replaces the module state set up by read_ip (source/input_param.f90:58-117),
  * get_combination (source/state_lists.f90:6-15) and mk_shift_{x,y,z}_SQ
@@ -94,6 +105,13 @@ int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where)
 /* Same product with complex(4) vectors (FP32 Krylov storage). */
 int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* where);
 
+/* The same product on real vectors (D doubles) for sectors whose H is real
+ * symmetric: chains at k = 0 and U(1) sectors (QS3G_ENOTSUP otherwise).
+ * Equals the real part of qs3g_hv applied to (v1, 0), bit for bit, at one
+ * FP64 FMA per hop instead of two.  No counterpart in the reference, whose
+ * vectors are complex(8) for every sector. */
+int qs3g_hv_real(qs3g_handle h, double* v0, const double* v1, const int* where);
+
 /* Schedule of the H*v kernel for the current general-lattice sector (chains
  * and U(1) sectors use one thread per row always): 0 = autotune (the first
  * product of each precision times a warp per row, lanes over the
@@ -131,6 +149,8 @@ int qs3g_connection_table_rows(qs3g_handle h, const int64_t* row_first, const in
  *            2 = complex(8) storage; dots, reorthogonalisation and restarts in
  *            double-float arithmetic on the FP32 pipe (about 2^-47 relative
  *            per operation; GB300 issues FP64 at 1/64 of the FP32 rate).
+ *            + QS3G_REAL: real vectors (k = 0 chains, U(1) sectors; else
+ *            QS3G_ENOTSUP).
  * conv_mode: 0 = the reference's test (|E_prev/E - 1| < tol on two consecutive
  *            restarts, eigen_solver.f90:150-159);
  *            1 = Ritz residual |beta_NOM C(NOM,j)| <= tol for j = 1..NOE.
