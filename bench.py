@@ -299,7 +299,8 @@ def solve_bench(args):
     ||r|| <= tol: plain FP64 TRLan from a random start, complex(4) storage +
     refinement from a random start, and the same from the network's start
     vector (trained here on chains L = 48..128 whose ground states the GPU
-    TRLan computes first)."""
+    TRLan computes first), with complex and with real Krylov vectors (k = 0:
+    H is real symmetric)."""
     from ed_gb300 import capi, learned
     delta, j2 = J1[1], J2[0]
     out = {"workload": f"xxz_chain_L{args.L}_Ndown4_k0_Delta{delta}_J2_{j2}", "tol": args.tol,
@@ -316,7 +317,8 @@ def solve_bench(args):
     t0 = time.perf_counter()
     v = learned.start_vector(net, h, delta, j2)
     out["network"]["predict_s"] = time.perf_counter() - t0
-    runs = [("fp32store_learned", 1, v), ("fp32store_random", 1, None), ("fp64_random", 0, None)]
+    runs = [("fp32store_real_learned", 1 | capi.REAL, v), ("fp32store_learned", 1, v),
+            ("fp32store_random", 1, None), ("fp64_random", 0, None)]
     psi = None
     for name, prec, start in runs:
         t0 = time.perf_counter()
@@ -331,6 +333,7 @@ def solve_bench(args):
     e64 = out["fp64_random"]["E0"]
     for name, _, _ in runs:
         out[name]["dE_vs_fp64"] = abs(out[name]["E0"] - e64)
+    out["speedup_learned_fp32_real_vs_fp64"] = out["fp64_random"]["seconds"] / out["fp32store_real_learned"]["seconds"]
     out["speedup_learned_fp32_vs_fp64"] = out["fp64_random"]["seconds"] / out["fp32store_learned"]["seconds"]
     out["sector_dim"] = D
     h.close()

@@ -6,9 +6,12 @@ Chain: nearest-neighbour (Jxy, Jz) = (1, delta), next-nearest (j2, j2),
 periodic, sector (nod, k).  The solver is qs3g_trlan with a residual stop
 (conv_mode 1: ||H psi - E psi|| <= tol, recomputed in FP64 at the end);
 precision 0 = FP64 throughout, 1 = complex(4) storage + refinement,
-2 = complex(8) storage with double-float arithmetic.  --learned trains the
-start-vector network first (ed_gb300.learned) and starts from its prediction
-(k = 0, nod <= 4).
+2 = complex(8) storage with double-float arithmetic; --real adds QS3G_REAL
+(real Krylov vectors; k = 0 only, where H is real symmetric).  --learned
+trains the start-vector network first (ed_gb300.learned) and starts from its
+prediction (k = 0, nod <= 4).
+
+    python -m ed_gb300.solve --L 1000 --precision 1 --real --learned
 """
 from __future__ import annotations
 
@@ -35,23 +38,24 @@ def main(argv=None):
     ap.add_argument("--maxitr", type=int, default=40000, help="cap on thick-restart cycles per phase")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--learned", action="store_true")
+    ap.add_argument("--real", action="store_true", help="real Krylov vectors (k = 0)")
     a = ap.parse_args(argv)
     h = learned.chain_handle(a.L, a.delta, a.j2)
     t0 = time.perf_counter()
     D = h.build_sector(a.nod, (a.k, 0, 0))
-    out = dict(L=a.L, nod=a.nod, k=a.k, delta=a.delta, j2=a.j2, D=D, precision=a.precision,
+    out = dict(L=a.L, nod=a.nod, k=a.k, delta=a.delta, j2=a.j2, D=D, precision=a.precision, real=a.real,
                build_s=time.perf_counter() - t0)
     start = None
     if a.learned:
         t0 = time.perf_counter()
         net = capi.Mlp(seed=1)
         learned.generate(net, learned.training_problems(seed=1))
-        learned.train(net)
+        learned.train(net, rounds=10, steps=300)
         start = learned.start_vector(net, h, a.delta, a.j2)
         out["learned_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     r = h.trlan(1, a.nok, a.nom, maxitr=a.maxitr, tol=a.tol, precision=a.precision, conv_mode=1, seed=a.seed,
-                start=start, want_psi=start is not None, allow_unconverged=True)
+                start=start, want_psi=start is not None, allow_unconverged=True, real=a.real)
     out.update(solve_s=time.perf_counter() - t0, hv=r["iters"], E0=float(r["ene"][0]), resid=float(r["resid"][0]),
                converged=bool(r["converged"]))
     if start is not None:
