@@ -142,7 +142,8 @@ __global__ void k_axpy(T* __restrict__ y, const T* __restrict__ x, int64_t n, co
 
 // ---------------------------------------------------------------- block GEMV for reorthogonalisation
 // part[c*nb + b] = sum over slice of conj(V[:,c]) w   for c < ncols (chunks of 8 columns)
-template <class T>
+// RE: real vectors two rows per slot -- only the real part is accumulated
+template <class T, bool RE>
 __global__ void __launch_bounds__(kRedThreads) k_gemv_h_part(const T* __restrict__ V, int64_t ldv, int ncols,
                                                              const T* __restrict__ w, int64_t n, double2* part) {
   __shared__ double2 sh[kRedThreads];
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(kRedThreads) k_gemv_h_part(const T* __restrict
           const T a = V[(int64_t)(c0 + k) * ldv + i];
           const double ar = Ld<T>::re(a), ai = Ld<T>::im(a);
           acc[k].x = fma(ar, br, fma(ai, bi, acc[k].x));
-          acc[k].y = fma(ar, bi, fma(-ai, br, acc[k].y));
+          if constexpr (!RE) acc[k].y = fma(ar, bi, fma(-ai, br, acc[k].y));
         }
       }
     }
@@ -189,8 +190,8 @@ __global__ void __launch_bounds__(kRedThreads) k_gemv_final(const double2* part,
   if (threadIdx.x == 0) out[c] = real ? make_double2(s.x, 0.0) : s;
 }
 
-// w -= V[:, :ncols] * coef   (coef from device memory)
-template <class T>
+// w -= V[:, :ncols] * coef   (coef from device memory; RE: coef real)
+template <class T, bool RE>
 __global__ void k_gemv_sub(const T* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
                            T* __restrict__ w, int64_t n) {
   __shared__ double2 c[128];
@@ -201,8 +202,13 @@ __global__ void k_gemv_sub(const T* __restrict__ V, int64_t ldv, int ncols, cons
     double re = (double)wv.x, im = (double)wv.y;
     for (int k = 0; k < ncols; ++k) {
       const T a = V[(int64_t)k * ldv + i];
-      re -= c[k].x * (double)a.x - c[k].y * (double)a.y;
-      im -= c[k].x * (double)a.y + c[k].y * (double)a.x;
+      if constexpr (RE) {
+        re -= c[k].x * (double)a.x;
+        im -= c[k].x * (double)a.y;
+      } else {
+        re -= c[k].x * (double)a.x - c[k].y * (double)a.y;
+        im -= c[k].x * (double)a.y + c[k].y * (double)a.x;
+      }
     }
     T o;
     o.x = (decltype(o.x))re;
@@ -213,7 +219,8 @@ __global__ void k_gemv_sub(const T* __restrict__ V, int64_t ldv, int ncols, cons
 
 // In-place restart V[:, :nok] = V[:, :nom] * C (zgemm + zcopy, eigen_solver.f90:147-149).
 // 32 rows per block; the rows' nom inputs are staged in shared memory first.
-template <class T>
+// RE: C real.
+template <class T, bool RE>
 __global__ void __launch_bounds__(256) k_restart(T* V, int64_t ldv, int nom, int nok, const double2* __restrict__ C,
                                                  int64_t n) {
   extern __shared__ double2 sm[];
@@ -239,8 +246,13 @@ __global__ void __launch_bounds__(256) k_restart(T* V, int64_t ldv, int nom, int
       double re = 0.0, im = 0.0;
       for (int j = 0; j < nom; ++j) {
         const double2 a = tile[j * 32 + r], c = cs[(size_t)oc * nom + j];
-        re = fma(a.x, c.x, fma(-a.y, c.y, re));
-        im = fma(a.x, c.y, fma(a.y, c.x, im));
+        if constexpr (RE) {
+          re = fma(a.x, c.x, re);
+          im = fma(a.y, c.x, im);
+        } else {
+          re = fma(a.x, c.x, fma(-a.y, c.y, re));
+          im = fma(a.x, c.y, fma(a.y, c.x, im));
+        }
       }
       T o;
       o.x = (decltype(o.x))re;
@@ -374,7 +386,8 @@ __global__ void k_axpy32(float2* __restrict__ y, const float2* __restrict__ x, i
   }
 }
 
-// w -= V[:, :ncols] * coef, coef split into float pairs in shared memory
+// w -= V[:, :ncols] * coef, coef split into float pairs in shared memory (RE: coef real)
+template <bool RE>
 __global__ void k_gemv_sub32(const float2* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
                              float2* __restrict__ w, int64_t n) {
   __shared__ float4 c[128];  // (re hi, re lo, im hi, im lo)
@@ -389,16 +402,23 @@ __global__ void k_gemv_sub32(const float2* __restrict__ V, int64_t ldv, int ncol
     for (int k = 0; k < ncols; ++k) {
       const float2 a = V[(int64_t)k * ldv + i];
       const float4 ck = c[k];
-      rlo = fmaf(-ck.y, a.x, rlo); rlo = fmaf(ck.w, a.y, rlo);
-      ilo = fmaf(-ck.y, a.y, ilo); ilo = fmaf(-ck.w, a.x, ilo);
-      re = fmaf(-ck.x, a.x, re); re = fmaf(ck.z, a.y, re);
-      im = fmaf(-ck.x, a.y, im); im = fmaf(-ck.z, a.x, im);
+      rlo = fmaf(-ck.y, a.x, rlo);
+      ilo = fmaf(-ck.y, a.y, ilo);
+      re = fmaf(-ck.x, a.x, re);
+      im = fmaf(-ck.x, a.y, im);
+      if constexpr (!RE) {
+        rlo = fmaf(ck.w, a.y, rlo);
+        ilo = fmaf(-ck.w, a.x, ilo);
+        re = fmaf(ck.z, a.y, re);
+        im = fmaf(-ck.z, a.x, im);
+      }
     }
     w[i] = make_float2(re + rlo, im + ilo);
   }
 }
 
-// In-place restart for complex(4): double-float accumulation, split C.
+// In-place restart for complex(4): double-float accumulation, split C (RE: C real).
+template <bool RE>
 __global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int nom, int nok,
                                                    const double2* __restrict__ C, int64_t n) {
   extern __shared__ float4 sm4[];
@@ -423,12 +443,19 @@ __global__ void __launch_bounds__(256) k_restart32(float2* V, int64_t ldv, int n
       for (int j = 0; j < nom; ++j) {
         const float2 a = tile[j * 32 + r];
         const float4 c = cs[(size_t)oc * nom + j];
-        df_add_prod(rh, rl, a.x, c.x);
-        df_add_prod(rh, rl, -a.y, c.z);
-        df_add_prod(ih, il, a.x, c.z);
-        df_add_prod(ih, il, a.y, c.x);
-        rl = fmaf(a.x, c.y, fmaf(-a.y, c.w, rl));
-        il = fmaf(a.x, c.w, fmaf(a.y, c.y, il));
+        if constexpr (RE) {
+          df_add_prod(rh, rl, a.x, c.x);
+          df_add_prod(ih, il, a.y, c.x);
+          rl = fmaf(a.x, c.y, rl);
+          il = fmaf(a.y, c.y, il);
+        } else {
+          df_add_prod(rh, rl, a.x, c.x);
+          df_add_prod(rh, rl, -a.y, c.z);
+          df_add_prod(ih, il, a.x, c.z);
+          df_add_prod(ih, il, a.y, c.x);
+          rl = fmaf(a.x, c.y, fmaf(-a.y, c.w, rl));
+          il = fmaf(a.x, c.w, fmaf(a.y, c.y, il));
+        }
       }
       V[(int64_t)oc * ldv + i] = make_float2(rh + rl, ih + il);
     }
@@ -486,7 +513,7 @@ __global__ void __launch_bounds__(kRedThreads) k_nrm_part64e(const double2* __re
 // partial is a fixed-order block reduction: part[c * nchunk + r].
 constexpr int kGemvChunks = 304;
 
-template <class T>
+template <class T, bool RE>
 __global__ void __launch_bounds__(256) k_gemv_h3(const T* __restrict__ V, int64_t ldv, int ncols,
                                                  const T* __restrict__ w, int64_t n, int64_t rows, double2* part) {
   __shared__ double2 sh[256];
@@ -511,8 +538,10 @@ __global__ void __launch_bounds__(256) k_gemv_h3(const T* __restrict__ V, int64_
         const float2 ar = make_float2(av.x, av.y), ai = make_float2(av.z, av.w);
         df_fma(acc[k][0], acc[k][1], ar, br);
         df_fma(acc[k][0], acc[k][1], ai, bi);
-        df_fma(acc[k][2], acc[k][3], ar, bi);
-        df_fma(acc[k][2], acc[k][3], fneg2(ai), br);
+        if constexpr (!RE) {  // real vectors: the imaginary part is not needed
+          df_fma(acc[k][2], acc[k][3], ar, bi);
+          df_fma(acc[k][2], acc[k][3], fneg2(ai), br);
+        }
       }
     }
   }
@@ -527,7 +556,8 @@ __global__ void __launch_bounds__(256) k_gemv_h3(const T* __restrict__ V, int64_
 }
 
 // w -= V[:, :ncols] * coef: the sum over columns in double-float, one FP64
-// subtraction per component at the end
+// subtraction per component at the end (RE: coef real)
+template <bool RE>
 __global__ void k_gemv_sub64e(const double2* __restrict__ V, int64_t ldv, int ncols, const double2* __restrict__ coef,
                               double2* __restrict__ w, int64_t n) {
   __shared__ float4 c[128];  // (re hi, re lo, im hi, im lo)
@@ -544,9 +574,11 @@ __global__ void k_gemv_sub64e(const double2* __restrict__ V, int64_t ldv, int nc
       const float4 ck = c[k];
       const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
       df_fma(rh, rl, cr, ar);
-      df_fma(rh, rl, fneg2(ci), ai);
       df_fma(ih, il, cr, ai);
-      df_fma(ih, il, ci, ar);
+      if constexpr (!RE) {
+        df_fma(rh, rl, fneg2(ci), ai);
+        df_fma(ih, il, ci, ar);
+      }
     }
     double2 wv = w[i];
     wv.x -= djoin(rh, rl);
@@ -555,7 +587,8 @@ __global__ void k_gemv_sub64e(const double2* __restrict__ V, int64_t ldv, int nc
   }
 }
 
-// In-place restart V[:, :nok] = V[:, :nom] * C with split inputs in shared memory.
+// In-place restart V[:, :nok] = V[:, :nom] * C with split inputs in shared memory (RE: C real).
+template <bool RE>
 __global__ void __launch_bounds__(256) k_restart64e(double2* V, int64_t ldv, int nom, int nok,
                                                     const double2* __restrict__ C, int64_t n) {
   extern __shared__ float4 smx[];
@@ -589,9 +622,11 @@ __global__ void __launch_bounds__(256) k_restart64e(double2* V, int64_t ldv, int
         const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
         const float2 cr = make_float2(c.x, c.y), ci = make_float2(c.z, c.w);
         df_fma(rh, rl, ar, cr);
-        df_fma(rh, rl, fneg2(ai), ci);
-        df_fma(ih, il, ar, ci);
         df_fma(ih, il, ai, cr);
+        if constexpr (!RE) {
+          df_fma(rh, rl, fneg2(ai), ci);
+          df_fma(ih, il, ar, ci);
+        }
       }
       V[(int64_t)oc * ldv + i] = make_double2(djoin(rh, rl), djoin(ih, il));
     }
@@ -669,9 +704,12 @@ void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2
     const int64_t tiles = (n + 255) / 256;
     nb = (int)std::min<int64_t>(kGemvChunks, tiles);
     const int64_t rows = (tiles + nb - 1) / nb * 256;
-    k_gemv_h3<T><<<dim3((unsigned)((ncols + 3) / 4), (unsigned)nb), 256, 0, st>>>(V, ldv, ncols, w, n, rows, part);
+    const dim3 grid((unsigned)((ncols + 3) / 4), (unsigned)nb);
+    if (real) k_gemv_h3<T, true><<<grid, 256, 0, st>>>(V, ldv, ncols, w, n, rows, part);
+    else k_gemv_h3<T, false><<<grid, 256, 0, st>>>(V, ldv, ncols, w, n, rows, part);
   } else {
-    k_gemv_h_part<T><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+    if (real) k_gemv_h_part<T, true><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
+    else k_gemv_h_part<T, false><<<kRedBlocks, kRedThreads, 0, st>>>(V, ldv, ncols, w, n, part);
   }
   check_launch("k_gemv_h_part");
   k_gemv_final<<<ncols, kRedThreads, 0, st>>>(part, nb, ncols, ov, real ? 1 : 0);
@@ -681,28 +719,38 @@ void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2
 template <class T>
 void Ops<T>::gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n) {
   if (ncols <= 0) return;
-  if constexpr (kF32<T>) k_gemv_sub32<<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
-  else if (eft) k_gemv_sub64e<<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
-  else k_gemv_sub<T><<<stream_grid(n), 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  const unsigned g = stream_grid(n);
+  if constexpr (kF32<T>) {
+    if (real) k_gemv_sub32<true><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+    else k_gemv_sub32<false><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  } else if (eft) {
+    if (real) k_gemv_sub64e<true><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+    else k_gemv_sub64e<false><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  } else {
+    if (real) k_gemv_sub<T, true><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+    else k_gemv_sub<T, false><<<g, 256, 0, st>>>(V, ldv, ncols, coef, w, n);
+  }
   check_launch("k_gemv_sub");
 }
+// launch an in-place restart kernel with sm bytes of dynamic shared memory
+template <class K, class... A>
+static void launch_restart(K kernel, size_t sm, int64_t n, cudaStream_t st, A... args) {
+  if (sm > 48 * 1024)
+    QS3G_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  kernel<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(args...);
+}
+
 template <class T>
 void Ops<T>::restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int64_t n) {
   if constexpr (kF32<T>) {
     const size_t sm = (size_t)nom * nok * sizeof(float4) + (size_t)nom * 32 * sizeof(float2);
-    if (sm > 48 * 1024)
-      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_restart32<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+    launch_restart(real ? k_restart32<true> : k_restart32<false>, sm, n, st, V, ldv, nom, nok, C, n);
   } else if (eft) {
     const size_t sm = ((size_t)nom * nok + (size_t)nom * 32) * sizeof(float4);
-    if (sm > 48 * 1024)
-      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart64e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_restart64e<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+    launch_restart(real ? k_restart64e<true> : k_restart64e<false>, sm, n, st, V, ldv, nom, nok, C, n);
   } else {
     const size_t sm = ((size_t)nom * 32 + (size_t)nom * nok) * sizeof(double2);
-    if (sm > 48 * 1024)
-      QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_restart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_restart<T><<<(unsigned)((n + 31) / 32), 256, sm, st>>>(V, ldv, nom, nok, C, n);
+    launch_restart(real ? k_restart<T, true> : k_restart<T, false>, sm, n, st, V, ldv, nom, nok, C, n);
   }
   check_launch("k_restart");
 }

@@ -42,3 +42,14 @@ def test_library_is_sm103a_only():
 def test_binding_covers_the_header():
     from ed_gb300 import capi
     assert sorted(capi.EXPORTS) == declared()
+
+
+def test_binding_constants_match_the_header():
+    """Status codes, vector locations and the QS3G_REAL flag have the header's values."""
+    from ed_gb300 import capi
+    text = open(os.path.join(ROOT, "include", "qs3g.h")).read()
+    consts = {k: int(v) for k, v in re.findall(r"\b(QS3G_[A-Z_0-9]+)\s*=\s*(\d+)", text)}
+    assert consts["QS3G_REAL"] == capi.REAL
+    assert consts["QS3G_HOST"] == capi.HOST and consts["QS3G_DEVICE"] == capi.DEVICE
+    for name in ("OK", "EINVAL", "ESTATE", "ERANGE", "ENOTSUP", "EBREAKDOWN", "ENOTCONV"):
+        assert consts["QS3G_" + name] == getattr(capi, name), name
