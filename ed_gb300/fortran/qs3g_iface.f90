@@ -136,5 +136,84 @@ module qs3g_iface
       integer(c_int) :: nlines, ex_i, itr, append
       real(c_double) :: alpha(*), beta2(*), norm1, E0, sztot
     end function
+
+    integer(c_int) function qs3g_read_alpha_beta(path, cap, alpha, beta2, norm1, E0, sztot, nlines) &
+        bind(C, name="qs3g_read_alpha_beta")
+      import :: c_int, c_char, c_double
+      character(kind=c_char) :: path(*)
+      integer(c_int) :: cap, nlines
+      real(c_double) :: alpha(*), beta2(*), norm1(*), E0(*), sztot(*)
+    end function
+
+    ! energy.dat lines (write / read back for re_wf = 1)
+    integer(c_int) function qs3g_write_energy(path, NOE, ene) bind(C, name="qs3g_write_energy")
+      import :: c_int, c_char, c_double
+      character(kind=c_char) :: path(*)
+      integer(c_int) :: NOE
+      real(c_double) :: ene(*)
+    end function
+
+    integer(c_int) function qs3g_read_energy(path, NOE, ene) bind(C, name="qs3g_read_energy")
+      import :: c_int, c_char, c_double
+      character(kind=c_char) :: path(*)
+      integer(c_int) :: NOE
+      real(c_double) :: ene(*)
+    end function
+
+    ! calcu_Sq_a alone: the new sector's list_s and S^a(q)|psi>
+    integer(c_int) function qs3g_sq_a(h, psi, spsmsz, qvec, Spos, D_new, list_s_new, fn) bind(C, name="qs3g_sq_a")
+      import :: c_ptr, c_int, c_int64_t, c_double, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: psi(*), fn(*)
+      integer(c_int) :: spsmsz
+      real(c_double) :: qvec(3), Spos(3, *)
+      integer(c_int64_t) :: D_new, list_s_new(*)
+    end function
+
+    ! ALG = 3: Full_diag_routines + make_full_hamiltonian + fulldia_routines_with_momentum
+    integer(c_int) function qs3g_full_diag(h, ene, psi) bind(C, name="qs3g_full_diag")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: h
+      real(c_double) :: ene(*)
+      complex(c_double_complex) :: psi(*)
+    end function
+
+    integer(c_int) function qs3g_full_hamiltonian(h, ham) bind(C, name="qs3g_full_hamiltonian")
+      import :: c_ptr, c_int, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: ham(*)
+    end function
+
+    ! DSFLan from a code that cannot allocate device memory
+    integer(c_int) function qs3g_cfrac_noalloc(nq, ldab, nlev, alpha, beta2, norm1, E0, eta, nomega, omega, &
+        compat, S) bind(C, name="qs3g_cfrac_noalloc")
+      import :: c_int, c_double
+      integer(c_int) :: nq, ldab, nlev(*), nomega, compat
+      real(c_double) :: alpha(*), beta2(*), norm1(*), E0(*), eta, omega(*), S(*)
+    end function
+
+    ! message of the handle's last failed call (c_null_ptr: the last global
+    ! failure, e.g. of the file routines); a NUL-terminated C string, see
+    ! qs3g_error_message below
+    type(c_ptr) function qs3g_last_error(h) bind(C, name="qs3g_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
   end interface
+
+contains
+
+  ! The last error message as a Fortran string (blank-padded to len(msg)).
+  subroutine qs3g_error_message(h, msg)
+    type(c_ptr), value :: h
+    character(len=*), intent(out) :: msg
+    character(kind=c_char), pointer :: c(:)
+    integer :: i
+    msg = ' '
+    call c_f_pointer(qs3g_last_error(h), c, [len(msg)])
+    do i = 1, len(msg)
+      if (c(i) == c_null_char) exit
+      msg(i:i) = c(i)
+    end do
+  end subroutine
 end module qs3g_iface
