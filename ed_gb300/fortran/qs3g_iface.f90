@@ -1,8 +1,8 @@
 ! qs3g_iface.f90 -- iso_c_binding interface of libqs3g.so for the QS3 Fortran
 ! sources.  A QS3 build links -lqs3g and `use qs3g_iface`; the bodies of the
-! routines listed in each comment are then replaced by these calls (see
-! INTEGRATION.md).  Every function returns 0 on success.  Scalars are passed
-! by reference, arrays as Fortran arrays (contiguous, column-major).
+! routines named in each comment then become these calls.  Every function
+! returns 0 on success.  Scalars are passed by reference, arrays as Fortran
+! arrays (contiguous, column-major).
 module qs3g_iface
   use iso_c_binding
   implicit none
