@@ -3,8 +3,8 @@
 This module loads ``oracle/_build/libqs3oracle.so`` (compiled from
 ``qs3_oracle.cpp`` by :func:`build`) and wraps its functions with numpy
 arrays.  Only the tests, ``__graft_entry__.smoke()`` and the CPU legs of
-``bench.py`` use it, and only as the checker / CPU baseline; the product
-library never imports it.
+``bench.py`` use it, and only to compare against or as the CPU baseline;
+the product library never imports it.
 
 Each wrapper names the QS3 routine it restates (paths relative to the
 QS-Cube/ED source tree).
