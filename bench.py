@@ -147,6 +147,12 @@ def chain_lists_cpu(nthreads):
     return O.chain_sector_lists(L_SITES, NOD, 0, nthreads)
 
 
+def workload_config(D, world):
+    """The workload as both arms name it (the reference arm and the GPU arm print the same dict)."""
+    return {"workload": WORKLOAD, "sector_dim": int(D), "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (x, y 16*D bytes each), no flush"}
+
+
 def run_reference(args, rank, world, dist):
     from oracle import oracle as O
     if rank != 0:
@@ -182,7 +188,7 @@ def run_reference(args, rank, world, dist):
         "impl": "reference", "metric": "hv_algorithmic_hbm_gbs", "value": value, "unit": "GB/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sector_dim": D},
+        "data": "synthetic", "config": workload_config(D, world),
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -252,9 +258,9 @@ def run_gpu(args, rank, world, local_rank, dist):
         "metric": "hv_algorithmic_hbm_gbs", "value": value, "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sector_dim": D, "nnz_offdiag": nnz,
-                   "bytes_per_hv": B, "l2": "inputs larger than L2 (x, y 663 MB each), no flush",
-                   "parallelism": f"replicas{world}", "sector_build_s": t_build},
+        "config": workload_config(D, world),
+        "hv_bytes": {"nnz_offdiag": nnz, "bytes_per_hv": B, "per_row": 48, "per_offdiag_entry": 24},
+        "sector_build_s": t_build,
         "hv_per_s": world * 1e3 / ms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
@@ -266,26 +272,9 @@ def run_gpu(args, rank, world, local_rank, dist):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:
-        nthreads = os.cpu_count() or 1
-        ls, lr = h.get_sector()
-        from oracle import oracle as O
-        om = O.Model(L_SITES, L_SITES, 1, 1, bonds, jxy, jz, kmax=NOD + 2)
-        sec = O.Sector(om, NOD, (0, 0, 0), ls, lr)
-        xc = x.cpu().numpy()
-        r0 = D // 3
-        t0 = time.perf_counter()
-        sec.hv(xc, rows=(r0, r0 + 2000), nthreads=nthreads)
-        per_row = (time.perf_counter() - t0) / 2000
-        rows = int(max(2000, min(D - r0, args.cpu_seconds / per_row)))
-        nnz_rows = O.count_offdiag_rows(sec, r0, r0 + rows, nthreads)
-        t0 = time.perf_counter()
-        sec.hv(xc, rows=(r0, r0 + rows), nthreads=nthreads)
-        tc = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": (rows * 48 + nnz_rows * 24) / tc / 1e9, "unit": "GB/s",
-                                "cores": nthreads, "kind": "port",
-                                "sample": f"{rows} rows of {D} timed, extrapolated per byte"}
+        line["cpu_baseline"], line["parity"] = cpu_leg(args, h, x, y, D)
     h.close()
-    if args.solve and rank == 0:
+    if args.solve and rank == 0 and world == 1:
         line["gs_solve"] = solve_bench(args)
     if args.dsf and rank == 0:
         line["dsf_batch"] = dsf_bench()
@@ -293,18 +282,74 @@ def run_gpu(args, rank, world, local_rank, dist):
         print(json.dumps(line), flush=True)
 
 
+def cpu_leg(args, h, x, y, D):
+    """The oracle on this host's cores: (1) timed on a bounded sample of rows
+    (cpu_baseline, extrapolated per byte); (2) the parity of the timed GPU
+    product on the same rows -- the oracle's own enumeration of the sector
+    (list_s bit for bit, list_r), its ham_to_vec_wave_vector on the sampled
+    rows against the GPU y of the timed region (same x), and the connection
+    table of 2,000 rows bit for bit."""
+    from oracle import oracle as O
+    from ed_gb300 import inputs
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ls, lr = O.chain_sector_lists(L_SITES, NOD, 0, nthreads)
+    t_lists = time.perf_counter() - t0
+    lsg, lrg = h.get_sector()
+    bonds, jxy, jz = inputs.chain_bonds(L_SITES, J1, J2)
+    om = O.Model(L_SITES, L_SITES, 1, 1, bonds, jxy, jz, kmax=NOD + 2)
+    sec = O.Sector(om, NOD, (0, 0, 0), ls, lr)
+    xc = x.cpu().numpy()
+    r0 = D // 3
+    t0 = time.perf_counter()
+    sec.hv(xc, rows=(r0, r0 + 2000), nthreads=nthreads)
+    per_row = (time.perf_counter() - t0) / 2000
+    rows = int(max(2000, min(D - r0, args.cpu_seconds / per_row)))
+    nnz_rows = O.count_offdiag_rows(sec, r0, r0 + rows, nthreads)
+    t0 = time.perf_counter()
+    yc = sec.hv(xc, rows=(r0, r0 + rows), nthreads=nthreads)[r0:r0 + rows]
+    tc = time.perf_counter() - t0
+    cpu = {"value": (rows * 48 + nnz_rows * 24) / tc / 1e9, "unit": "GB/s", "cores": nthreads,
+           "kind": "port", "sample": f"{rows} rows of {D} timed (rows {r0}..{r0 + rows - 1}), "
+                                     f"extrapolated per byte"}
+    yg = y[r0:r0 + rows].cpu().numpy()
+    err = float(np.abs(yg - yc).max() / np.abs(yc).max())
+    c0, c1 = D // 5, D // 5 + 2000
+    ro, co, eo, bo = sec.connection_table(nthreads, rows=(c0, c1))
+    rg, cg, eg, bg = h.connection_table(rows=(c0, c1))
+    table_equal = bool(np.array_equal(rg, ro + 1) and np.array_equal(cg, co + 1) and
+                       np.array_equal(eg, eo) and np.array_equal(bg, bo + 1))
+    parity = {"oracle": "CPU restatement of ham_to_vec_wave_vector / representative_SQ / findstate",
+              "list_s_equal": bool(np.array_equal(lsg, ls)),
+              "list_r_max_rel_err": float(np.abs(lrg / lr - 1.0).max()),
+              "hv_rows": rows, "hv_max_rel_err": err, "hv_tol": 1e-13,
+              "table_rows": c1 - c0, "table_entries": int(len(ro)), "table_bit_exact": table_equal,
+              "oracle_lists_s": t_lists}
+    parity["ok"] = bool(parity["list_s_equal"] and parity["list_r_max_rel_err"] <= 1e-15 and
+                        err <= 1e-13 and table_equal)
+    return cpu, parity
+
+
 def solve_bench(args):
-    """Ground state of the benchmark chain (L, N_down=4, k=0, Delta=0.5,
-    J2=0.3; an unseen point of the network's training range) to
-    ||r|| <= tol: plain FP64 TRLan from a random start, complex(4) storage +
-    refinement from a random start, and the same from the network's start
-    vector (trained here on chains L = 48..128 whose ground states the GPU
-    TRLan computes first), with complex and with real Krylov vectors (k = 0:
-    H is real symmetric)."""
+    """Ground state of the benchmark chain (L, N_down=4, k=0, Delta=0.5, J2=0.3,
+    an unseen point of the network's training range) to ||H psi - E psi|| <= tol,
+    the residual recomputed in FP64 from the returned vector:
+
+      learned_fp32_real  the network's start vector (trained here on chains
+                         L = 48..128 whose ground states the GPU TRLan computes
+                         first), complex(4) Krylov storage with FP64-accurate
+                         reductions and refinement, real vectors (k = 0: H is
+                         real symmetric);
+      plain_fp64_random  the reference's arithmetic: complex(8) vectors, FP64
+                         throughout, random start (eigen_solver.f90:92-96),
+                         stopped at plain_limit seconds if it has not converged.
+    --solve-all adds the same start and storage with complex vectors, complex(4)
+    storage from a random start, FP64 real vectors from a random start and
+    double-float arithmetic from a random start."""
     from ed_gb300 import capi, learned
     delta, j2 = J1[1], J2[0]
     out = {"workload": f"xxz_chain_L{args.L}_Ndown4_k0_Delta{delta}_J2_{j2}", "tol": args.tol,
-           "NOK": args.nok, "NOM": args.nom}
+           "NOK": args.nok, "NOM": args.nom, "conv": "FP64-recomputed residual <= tol"}
     t0 = time.perf_counter()
     net = capi.Mlp(seed=1)
     learned.generate(net, learned.training_problems(seed=1))
@@ -317,24 +362,42 @@ def solve_bench(args):
     t0 = time.perf_counter()
     v = learned.start_vector(net, h, delta, j2)
     out["network"]["predict_s"] = time.perf_counter() - t0
-    runs = [("fp32store_real_learned", 1 | capi.REAL, v), ("fp32store_learned", 1, v),
-            ("fp32store_random", 1, None), ("fp64_random", 0, None)]
+    runs = [("learned_fp32_real", 1 | capi.REAL, v, 0.0)]
+    if args.solve_all:
+        runs += [("learned_fp32", 1, v, 0.0), ("random_fp32", 1, None, 0.0),
+                 ("random_fp64_real", 0 | capi.REAL, None, 0.0), ("random_df", 2, None, 0.0)]
+    runs.append(("plain_fp64_random", 0, None, args.plain_limit))
     psi = None
-    for name, prec, start in runs:
+    for name, prec, start, limit in runs:
+        h.set_time_limit(limit)
         t0 = time.perf_counter()
         r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec, conv_mode=1,
                     seed=7, start=start, want_psi=psi is None, allow_unconverged=True)
         dt = time.perf_counter() - t0
+        st = h.trlan_stats()
         if psi is None:
             psi = r["psi"][0]
             out["learned_start_overlap"] = float(abs(np.vdot(psi, v)) / np.linalg.norm(v))
-        out[name] = {"seconds": dt, "hv": r["iters"], "E0": float(r["ene"][0]),
-                     "resid": float(r["resid"][0]), "converged": bool(r["converged"])}
-    e64 = out["fp64_random"]["E0"]
-    for name, _, _ in runs:
-        out[name]["dE_vs_fp64"] = abs(out[name]["E0"] - e64)
-    out["speedup_learned_fp32_real_vs_fp64"] = out["fp64_random"]["seconds"] / out["fp32store_real_learned"]["seconds"]
-    out["speedup_learned_fp32_vs_fp64"] = out["fp64_random"]["seconds"] / out["fp32store_learned"]["seconds"]
+        nhv = st["hv_fp32"] + st["hv_fp64"]
+        out[name] = {"seconds": dt, "hv": r["iters"], "hv_fp32": st["hv_fp32"], "hv_fp64": st["hv_fp64"],
+                     "fp32_share": st["hv_fp32"] / max(1, nhv), "restarts": st["restarts"],
+                     "E0": float(r["ene"][0]), "resid": float(r["resid"][0]), "converged": bool(r["converged"]),
+                     "timed_out": st["timed_out"], "ms_per_hv": 1e3 * dt / max(1, nhv)}
+    h.set_time_limit(0.0)
+    ref = out["plain_fp64_random"]
+    for name, _, _, _ in runs:
+        out[name]["dE_vs_plain_fp64"] = abs(out[name]["E0"] - ref["E0"])
+    head = out["learned_fp32_real"]
+    # a plain run stopped at its time limit gives a lower bound on the speed-up
+    out["speedup_learned_fp32_real_vs_plain_fp64"] = ref["seconds"] / head["seconds"]
+    out["speedup_is_lower_bound"] = bool(ref["timed_out"] or not ref["converged"])
+    out["target_met"] = bool(head["converged"] and head["resid"] <= args.tol and
+                             (out["speedup_is_lower_bound"] or head["dE_vs_plain_fp64"] <= 1e-10) and
+                             out["speedup_learned_fp32_real_vs_plain_fp64"] >= 2.0)
+    if args.solve_all:
+        out["speedup_learned_fp32_vs_plain_fp64"] = ref["seconds"] / out["learned_fp32"]["seconds"]
+        out["speedup_learned_vs_random_fp64_real"] = (out["random_fp64_real"]["seconds"] /
+                                                      head["seconds"])
     out["sector_dim"] = D
     h.close()
     return out
@@ -385,13 +448,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--solve", action="store_true",
-                    help="add the ground-state solves (learned start + complex(4) storage vs plain FP64); minutes")
+    ap.add_argument("--no-solve", dest="solve", action="store_false",
+                    help="skip the ground-state solves (learned start + complex(4) storage vs plain FP64 "
+                         "random start; about 20 minutes, on by default)")
+    ap.add_argument("--solve-all", action="store_true",
+                    help="with the solves, also the complex-vector, random-start and real FP64 arms")
     ap.add_argument("--dsf", action="store_true", help="add the all-q DSF batch (L=200, 200 q, 150 levels)")
     ap.add_argument("--nok", type=int, default=16)
     ap.add_argument("--nom", type=int, default=48)
     ap.add_argument("--maxrestart", type=int, default=40000)
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--plain-limit", type=float, default=1200.0,
+                    help="wall seconds after which the plain FP64 solve stops (reported as a lower bound)")
     ap.add_argument("--L", type=int, default=1000,
                     help="chain length (1000 is the benchmark; smaller sizes are for profiling)")
     args = ap.parse_args()

@@ -35,7 +35,8 @@ EXPORTS = [
     "qs3g_full_hamiltonian", "qs3g_full_diag",
     "qs3g_mlp_create", "qs3g_mlp_destroy", "qs3g_mlp_params", "qs3g_mlp_add_sample", "qs3g_mlp_clear",
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
-    "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real",
+    "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real", "qs3g_set_time_limit", "qs3g_trlan_stats",
+    "qs3g_build_sector_i32", "qs3g_get_sector_i32", "qs3g_load_sector", "qs3g_load_sector_i32",
 ]
 
 MLP_NPARAMS = 35329
@@ -153,6 +154,38 @@ class Handle:
         self.nod = int(nod)
         return self.D
 
+    def build_sector_i32(self, nod, K=(0, 0, 0)):
+        """qs3g_build_sector_i32: THS as a default-kind (32-bit) integer."""
+        D = C.c_int()
+        _check(load().qs3g_build_sector_i32(self.h, _i(nod), _i(K[0]), _i(K[1]), _i(K[2]), C.byref(D)), self.h)
+        self.D = int(D.value)
+        self.nod = int(nod)
+        return self.D
+
+    def load_sector(self, nod, K, list_s, list_r, i32=False):
+        """qs3g_load_sector(_i32): adopt the caller's (list_s, list_r) of the (nod, K) sector."""
+        ls = np.ascontiguousarray(list_s, np.int32 if i32 else np.int64)
+        lr = np.ascontiguousarray(list_r, np.float64)
+        if ls.shape != lr.shape or ls.ndim != 1:
+            raise ValueError("list_s and list_r must be 1-D of the same length")
+        if i32:
+            rc = load().qs3g_load_sector_i32(self.h, _i(nod), _i(K[0]), _i(K[1]), _i(K[2]), _i(len(ls)), _ptr(ls),
+                                             _ptr(lr))
+        else:
+            n = C.c_int64(len(ls))
+            rc = load().qs3g_load_sector(self.h, _i(nod), _i(K[0]), _i(K[1]), _i(K[2]), C.byref(n), _ptr(ls),
+                                         _ptr(lr))
+        _check(rc, self.h)
+        self.D = len(ls)
+        self.nod = int(nod)
+        return self.D
+
+    def get_sector_i32(self):
+        ls = np.zeros(self.D, np.int32)
+        lr = np.zeros(self.D, np.float64)
+        _check(load().qs3g_get_sector_i32(self.h, _ptr(ls), _ptr(lr)), self.h)
+        return ls, lr
+
     def get_sector(self):
         ls = np.zeros(self.D, np.int64)
         lr = np.zeros(self.D, np.float64)
@@ -245,6 +278,19 @@ class Handle:
             _check(rc, self.h)
         return dict(ene=ene, psi=psi, iters=int(iters.value), resid=resid, converged=(rc == OK))
 
+    def set_time_limit(self, seconds):
+        """Wall-clock limit of later trlan calls on this handle (0 = none)."""
+        _check(load().qs3g_set_time_limit(self.h, _d(seconds)), self.h)
+
+    def trlan_stats(self):
+        """What the last trlan call did: H*v on complex(4) / complex(8) vectors, restarts, seconds."""
+        a, b, r, to = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        sec = C.c_double(0.0)
+        _check(load().qs3g_trlan_stats(self.h, C.byref(a), C.byref(b), C.byref(r), C.byref(sec), C.byref(to)),
+               self.h)
+        return dict(hv_fp32=int(a.value), hv_fp64=int(b.value), restarts=int(r.value), seconds=float(sec.value),
+                    timed_out=bool(to.value))
+
     def lanczos(self, maxitr=10000, minitr=20, itrint=5, tol=1e-14, seed=1, start=None):
         ene = np.zeros(1)
         psi = np.zeros(self.D, np.complex128)
@@ -304,15 +350,31 @@ def _correlations(h, psi):
 Handle.correlations = _correlations
 
 
-def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
-    """DSFLan continued fraction for nq spectra: alpha/beta2 are (nq, ldab)."""
+def _cfrac_args(alpha, beta2, nlev, norm1, E0, omega):
+    """Shape-checked contiguous copies of the continued-fraction inputs: alpha and
+    beta2 (nq, ldab), nlev / norm1 / E0 with nq entries (the C side reads nq of
+    each), omega 1-D."""
     alpha = np.ascontiguousarray(np.atleast_2d(alpha), np.float64)
     beta2 = np.ascontiguousarray(np.atleast_2d(beta2), np.float64)
-    nq, ld = alpha.shape
+    nq = alpha.shape[0]
     nlev = np.ascontiguousarray(np.atleast_1d(nlev), np.int32)
     norm1 = np.ascontiguousarray(np.atleast_1d(norm1), np.float64)
     E0 = np.ascontiguousarray(np.atleast_1d(E0), np.float64)
     omega = np.ascontiguousarray(omega, np.float64)
+    if beta2.shape != alpha.shape:
+        raise ValueError(f"beta2 has shape {beta2.shape}, alpha {alpha.shape}")
+    for name, a in (("nlev", nlev), ("norm1", norm1), ("E0", E0)):
+        if a.ndim != 1 or a.size != nq:
+            raise ValueError(f"{name} needs {nq} entries (one per spectrum), got shape {a.shape}")
+    if omega.ndim != 1:
+        raise ValueError("omega must be one-dimensional")
+    return alpha, beta2, nlev, norm1, E0, omega
+
+
+def cfrac(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
+    """DSFLan continued fraction for nq spectra: alpha/beta2 are (nq, ldab)."""
+    alpha, beta2, nlev, norm1, E0, omega = _cfrac_args(alpha, beta2, nlev, norm1, E0, omega)
+    nq, ld = alpha.shape
     S = np.zeros((nq, len(omega)))
     _check(load().qs3g_cfrac(_i(nq), _i(ld), _ptr(nlev), _ptr(alpha), _ptr(beta2), _ptr(norm1),
                              _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega), _i(1 if compat else 0),
@@ -324,18 +386,22 @@ def cfrac_noalloc(alpha, beta2, nlev, norm1, E0, eta, omega, compat=True):
     """qs3g_cfrac_noalloc: the same continued fraction, staged in the library's
     static device array instead of allocated buffers (for callers that cannot
     allocate device memory)."""
-    alpha = np.ascontiguousarray(np.atleast_2d(alpha), np.float64)
-    beta2 = np.ascontiguousarray(np.atleast_2d(beta2), np.float64)
+    alpha, beta2, nlev, norm1, E0, omega = _cfrac_args(alpha, beta2, nlev, norm1, E0, omega)
     nq, ld = alpha.shape
-    nlev = np.ascontiguousarray(np.atleast_1d(nlev), np.int32)
-    norm1 = np.ascontiguousarray(np.atleast_1d(norm1), np.float64)
-    E0 = np.ascontiguousarray(np.atleast_1d(E0), np.float64)
-    omega = np.ascontiguousarray(omega, np.float64)
     S = np.zeros((nq, len(omega)))
     _check(load().qs3g_cfrac_noalloc(_i(nq), _i(ld), _ptr(nlev), _ptr(alpha), _ptr(beta2), _ptr(norm1),
                                      _ptr(E0), _d(eta), _i(len(omega)), _ptr(omega),
                                      _i(1 if compat else 0), _ptr(S)))
     return S
+
+
+def cfrac_noalloc_doubles(nq, ldab, nomega):
+    """Doubles of the static area one qs3g_cfrac_noalloc call stages (each region
+    rounded up to 32 doubles): alpha and beta2 (nq*ldab each), norm1 and E0 (nq
+    each), omega, S (nq*nomega) and nlev (ceil(nq/2) doubles of int32 pairs).
+    The call is accepted when this is at most 524,288."""
+    up32 = lambda n: (n + 31) // 32 * 32
+    return (2 * up32(nq * ldab) + 2 * up32(nq) + up32(nomega) + up32(nq * nomega) + up32((nq + 1) // 2))
 
 
 def _full_hamiltonian(h):

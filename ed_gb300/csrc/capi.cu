@@ -190,6 +190,95 @@ int qs3g_get_sector(qs3g_handle h, int64_t* list_s, double* list_r) {
   });
 }
 
+// A sector the caller already enumerated (the Fortran's allocate_lists_omp_SQ):
+// the (NOD, K) sector is built on the GPU and compared with the caller's
+// lists -- D, list_s bit for bit, list_r to 1e-12 relative -- so that the
+// handle's rows are the caller's rows; a mismatch is QS3G_EINVAL naming the
+// first differing row.
+static int load_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, int64_t D,
+                       const int64_t* list_s, const double* list_r) {
+  QS3G_REQUIRE(h && NOD && KX && KY && KZ && list_s && list_r, QS3G_EINVAL, "null argument");
+  QS3G_REQUIRE(D >= 0, QS3G_EINVAL, "D must be >= 0");
+  const int K[3] = {*KX, *KY, *KZ};
+  std::unique_ptr<Sector> s(new Sector());
+  build_sector(h->model, *NOD, K, *s, h->stream);
+  QS3G_REQUIRE(s->D == D, QS3G_EINVAL,
+               "the caller's sector has " + std::to_string(D) + " rows, the (NOD, K) sector " +
+                   std::to_string(s->D));
+  if (D > 0) {
+    std::vector<int64_t> ls(D);
+    std::vector<double> lr(D);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(ls.data(), s->d_list_s.get(), D * 8, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(lr.data(), s->d_list_r.get(), D * 8, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    for (int64_t i = 0; i < D; ++i) {
+      QS3G_REQUIRE(list_s[i] == ls[i], QS3G_EINVAL,
+                   "list_s(" + std::to_string(i + 1) + ") differs from the (NOD, K) sector's");
+      QS3G_REQUIRE(std::fabs(list_r[i] - lr[i]) <= 1e-12 * std::fabs(lr[i]), QS3G_EINVAL,
+                   "list_r(" + std::to_string(i + 1) + ") differs from the (NOD, K) sector's");
+    }
+  }
+  h->sector = std::move(s);
+  return QS3G_OK;
+}
+
+int qs3g_load_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, const int64_t* D,
+                     const int64_t* list_s, const double* list_r) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(D, QS3G_EINVAL, "null argument");
+    return load_sector(h, NOD, KX, KY, KZ, *D, list_s, list_r);
+  });
+}
+
+int qs3g_load_sector_i32(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, const int* THS,
+                         const int* list_s, const double* list_r) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(THS && list_s && *THS >= 0, QS3G_EINVAL, "null argument or THS < 0");
+    const std::vector<int64_t> ls(list_s, list_s + *THS);
+    return load_sector(h, NOD, KX, KY, KZ, (int64_t)*THS, ls.data(), list_r);
+  });
+}
+
+int qs3g_build_sector_i32(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, int* THS) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h && NOD && KX && KY && KZ, QS3G_EINVAL, "null argument");
+    const int K[3] = {*KX, *KY, *KZ};
+    std::unique_ptr<Sector> s(new Sector());
+    build_sector(h->model, *NOD, K, *s, h->stream);
+    QS3G_REQUIRE(s->D <= INT32_MAX, QS3G_ERANGE,
+                 "the sector has " + std::to_string(s->D) + " rows, more than a default integer holds");
+    if (s->D > 0) {  // the largest code is the last row's
+      int64_t last = 0;
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(&last, s->d_list_s.get() + (s->D - 1), 8, cudaMemcpyDeviceToHost, h->stream));
+      QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+      QS3G_REQUIRE(last <= INT32_MAX, QS3G_ERANGE,
+                   "list_s codes reach " + std::to_string(last) + ", more than a default integer holds");
+    }
+    h->sector = std::move(s);
+    if (THS) *THS = (int)h->sector->D;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_get_sector_i32(qs3g_handle h, int* list_s, double* list_r) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(s.D <= INT32_MAX, QS3G_ERANGE, "the sector has more rows than a default integer holds");
+    if (s.D == 0) return QS3G_OK;
+    if (list_s) {
+      std::vector<int64_t> ls(s.D);
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(ls.data(), s.d_list_s.get(), s.D * 8, cudaMemcpyDeviceToHost, h->stream));
+      QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+      QS3G_REQUIRE(ls[s.D - 1] <= INT32_MAX, QS3G_ERANGE, "list_s codes exceed a default integer");
+      for (int64_t i = 0; i < s.D; ++i) list_s[i] = (int)ls[i];
+    }
+    if (list_r)
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(list_r, s.d_list_r.get(), s.D * 8, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
 // Device staging for the host-pointer forms of H*v: kept in the handle and
 // grown on demand, so repeated calls do not allocate.
 static void* staging(qs3g_ctx* h, int which, size_t bytes) {
@@ -340,8 +429,32 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
     QS3G_REQUIRE(p.conv_mode >= 0 && p.conv_mode <= 2, QS3G_EINVAL, "conv_mode must be 0, 1 or 2");
     const int sm = start_mode ? *start_mode : 0;
     QS3G_REQUIRE(sm == 0 || (sm == 1 && start), QS3G_EINVAL, "start_mode 1 needs a start vector");
+    p.time_limit = h->time_limit;
+    h->last_stats = TrlanStats();
     return trlan(h->model, s, p, sm == 1 ? reinterpret_cast<const double2*>(start) : nullptr, ene,
-                 reinterpret_cast<double2*>(psi), iters, resid, h->stream);
+                 reinterpret_cast<double2*>(psi), iters, resid, h->stream, &h->last_stats);
+  });
+}
+
+int qs3g_set_time_limit(qs3g_handle h, const double* seconds) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h && seconds && std::isfinite(*seconds) && *seconds >= 0.0, QS3G_EINVAL,
+                 "time limit must be finite and >= 0");
+    h->time_limit = *seconds;
+    return QS3G_OK;
+  });
+}
+
+int qs3g_trlan_stats(qs3g_handle h, int* hv_fp32, int* hv_fp64, int* restarts, double* seconds, int* timed_out) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h, QS3G_EINVAL, "null handle");
+    const TrlanStats& t = h->last_stats;
+    if (hv_fp32) *hv_fp32 = t.hv32;
+    if (hv_fp64) *hv_fp64 = t.hv64;
+    if (restarts) *restarts = t.restarts;
+    if (seconds) *seconds = t.seconds;
+    if (timed_out) *timed_out = t.timed_out ? 1 : 0;
+    return QS3G_OK;
   });
 }
 

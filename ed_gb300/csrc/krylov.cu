@@ -13,11 +13,13 @@
 // kernel launches with no host round trip; the host reads the scalars once
 // per restart to solve the NOM x NOM Ritz problem.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <mutex>
 #include <string>
 
@@ -25,6 +27,8 @@
 #include "qs3g_device.cuh"
 #include "qs3g_internal.cuh"
 #include "eft.cuh"
+#include <chrono>
+
 #include "krylov.h"
 
 namespace qs3g {
@@ -956,7 +960,12 @@ struct TrlanOut {
   int hv_count = 0;
   bool converged = false;
   int restarts = 0;
+  bool timed_out = false;
 };
+
+double wall_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 // FP64 residual of the Ritz pairs in V[:, :NOE] with Ritz values ene[0..NOE):
 // the largest, in the units of conv_mode.
@@ -973,7 +982,7 @@ template <class T>
 TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
                     double tol, int conv_mode, cudaStream_t st, Scratch& sc, int reorth_passes,
                     double shift = 0.0, bool eft = false, bool real = false, const RitzCheck& check = RitzCheck(),
-                    double target = 0.0) {
+                    double target = 0.0, double deadline = 0.0) {
   const int64_t D = real ? (s.D + 1) / 2 : s.D;  // T slots per vector
   Ops<T> ops{st, sc.part.get(), eft, real};
   double2* alpha = sc.scal;              // [NOM+2]
@@ -1061,6 +1070,10 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
       else if (++stall >= 20) break;
     }
     if (tritr == maxitr) break;
+    if (deadline > 0.0 && wall_seconds() > deadline) {
+      out.timed_out = true;
+      break;
+    }
     QS3G_CHECK_CUDA(cudaMemcpyAsync(col(NOK), col(NOM), D * sizeof(T), cudaMemcpyDeviceToDevice, st));
     for (int j = 0; j < NOK; ++j) calpha[j + 1] = ene[j];
     for (int j = 1; j <= NOK; ++j) cbeta[j] = cbeta[NOM] * Cc[(NOM - 1) + (size_t)(j - 1) * NOM];
@@ -1114,7 +1127,9 @@ void Scratch::ensure(int nom) {
 }
 
 int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
-          double2* h_psi, int* iters, double* resid, cudaStream_t st) {
+          double2* h_psi, int* iters, double* resid, cudaStream_t st, TrlanStats* stats) {
+  const double t_start = wall_seconds();
+  const double deadline = p.time_limit > 0.0 ? t_start + p.time_limit : 0.0;
   int NOM = p.NOM;
   const int NOE = p.NOE, NOK = p.NOK;
   QS3G_REQUIRE(NOE >= 1 && NOK >= 1 && NOE <= NOK, QS3G_EINVAL, "need 1 <= NOE <= NOK");
@@ -1134,8 +1149,9 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   };
   Scratch sc;
   sc.ensure(NOM);
-  int hv_total = 0;
-  std::vector<double> ene;
+  int hv_total = 0, restarts_total = 0;
+  bool timed_out = false;
+  std::vector<double> ene, ene_phase1;
   DevBuf<double2> d_start, d_pack;
   const double2* start64 = nullptr;
   if (h_start) {
@@ -1162,8 +1178,11 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     // the complex(4) phase runs on H - sigma, sigma = sum_b Jz_b/4 (the fully polarised energy): the
     // large common diagonal then does not enter the FP32 rounding of H*v
     TrlanOut r1 = trlan_core<float2>(m, s, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, st, sc,
-                                     p.reorth_passes, m.Sz_all, false, real);
+                                     p.reorth_passes, m.Sz_all, false, real, RitzCheck(), 0.0, deadline);
     hv_total += r1.hv_count;
+    restarts_total += r1.restarts;
+    timed_out = r1.timed_out;
+    ene_phase1 = r1.ene;
     // phase 2: FP64 thick-restart Lanczos from the sum of the NOE Ritz vectors
     Ops<double2> o64{st, sc.part.get()};
     f32_to_f64(V64.get(), V32.get(), n, st);
@@ -1215,15 +1234,15 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     };
   }
   TrlanOut r2;
-  for (int attempt = 0; attempt < 4; ++attempt) {
+  for (int attempt = 0; attempt < 4 && !timed_out; ++attempt) {
     const bool eft = p.precision != 0 && attempt < 2;
     if (attempt == 0) {
       r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st,
-                               sc, p.reorth_passes, 0.0, eft, real, check, p.tol);
+                               sc, p.reorth_passes, 0.0, eft, real, check, p.tol, deadline);
     } else {
       try {
         r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode,
-                                 st, sc, p.reorth_passes, 0.0, eft, real, check, p.tol);
+                                 st, sc, p.reorth_passes, 0.0, eft, real, check, p.tol, deadline);
       } catch (const Error& e) {
         // with NOE = 1 column 0 still holds the (normalised) previous Ritz
         // vector; with more, the other Ritz vectors were overwritten
@@ -1233,6 +1252,8 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
       }
     }
     hv_total += r2.hv_count;
+    restarts_total += r2.restarts;
+    timed_out = timed_out || r2.timed_out;
     if (p.conv_mode == 0 || !r2.converged) break;
     Ops<double2> o64{st, sc.part.get()};
     double worst = 0.0;
@@ -1263,6 +1284,9 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
                              hv_total - hv_phase1);
   converged = r2.converged;
   ene = r2.ene;
+  // a time limit reached in the complex(4) phase leaves that phase's Ritz values
+  if ((int)ene.size() < NOE) ene = ene_phase1;
+  if ((int)ene.size() < NOE) ene.assign(NOE, std::numeric_limits<double>::quiet_NaN());
   for (int j = 0; j < NOE; ++j) ene_out[j] = ene[j];
   if (iters) *iters = hv_total;
   // FP64 residuals ||H psi_j - E_j psi_j|| of the Ritz vectors in V[:, :NOE]
@@ -1291,6 +1315,13 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
       }
     }
     QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
+  if (stats) {
+    stats->hv32 = hv_phase1;
+    stats->hv64 = hv_total - hv_phase1;
+    stats->restarts = restarts_total;
+    stats->timed_out = timed_out;
+    stats->seconds = wall_seconds() - t_start;
   }
   return converged ? QS3G_OK : QS3G_ENOTCONV;
 }

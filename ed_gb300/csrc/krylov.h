@@ -91,6 +91,7 @@ struct TrlanParams {
   double tol32 = 0.0;     // phase-1 relative residual target (0: default 1e-5)
   int reorth_passes = 1;
   bool real = false;      // real Krylov vectors (real_sector(s) only)
+  double time_limit = 0;  // wall seconds; > 0: stop (not converged) at the first restart past it
 };
 
 // Thick-restart Lanczos on many chain sectors in lock step (batch_trlan.cu).
@@ -99,7 +100,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
                    const TrlanParams& p, double* ene, double* resid, int* hv, int* status, cudaStream_t st);
 
 int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
-          double2* h_psi, int* iters, double* resid, cudaStream_t st);
+          double2* h_psi, int* iters, double* resid, cudaStream_t st, TrlanStats* stats = nullptr);
 int lanczos(const Model& m, const Sector& s, int maxitr, int minitr, int itrint, double tol, const double2* h_start,
             uint64_t seed, double* ene_out, double2* h_psi, int* iters, cudaStream_t st);
 void cfrac(int nq, int ldab, const int* nlev, const double* alpha, const double* beta2, const double* norm1,

@@ -165,6 +165,15 @@ int64_t connection_table(const Model& m, const Sector& s, int64_t* row, int64_t*
 uint64_t binom_u64(int n, int k);
 int bits_for(int v);
 
+// What one thick-restart Lanczos call did: H*v products on complex(4) and on
+// complex(8) Krylov vectors (FP64 residual checks included), thick restarts,
+// wall time, and whether it stopped at its time limit.
+struct TrlanStats {
+  int hv32 = 0, hv64 = 0, restarts = 0;
+  double seconds = 0.0;
+  bool timed_out = false;
+};
+
 }  // namespace qs3g
 
 // the opaque handle
@@ -175,4 +184,6 @@ struct qs3g_ctx {
   bool own_stream = true;
   qs3g::DevBuf<char> stage[2];  // device staging of the host-pointer H*v forms
   std::string last_error;
+  double time_limit = 0.0;        // wall-clock limit of qs3g_trlan (qs3g_set_time_limit)
+  qs3g::TrlanStats last_stats;    // what the last qs3g_trlan on this handle did
 };

@@ -34,6 +34,57 @@ module qs3g_iface
       integer(c_int64_t) :: D
     end function
 
+    ! allocate_lists_omp_SQ with the reference's default-kind THS (main.f90:28-34);
+    ! QS3G_ERANGE when THS or a list_s code does not fit
+    integer(c_int) function qs3g_build_sector_i32(h, NOD, KX, KY, KZ, THS) bind(C, name="qs3g_build_sector_i32")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: h
+      integer(c_int) :: NOD, KX, KY, KZ
+      integer(c_int) :: THS
+    end function
+
+    integer(c_int) function qs3g_get_sector_i32(h, list_s, list_r) bind(C, name="qs3g_get_sector_i32")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: h
+      integer(c_int) :: list_s(*)
+      real(c_double) :: list_r(*)
+    end function
+
+    ! a sector the Fortran side enumerated itself (allocate_lists_omp_SQ): checked
+    ! against the (NOD, K) sector and adopted; default-kind and 64-bit forms
+    integer(c_int) function qs3g_load_sector_i32(h, NOD, KX, KY, KZ, THS, list_s, list_r) &
+        bind(C, name="qs3g_load_sector_i32")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: h
+      integer(c_int) :: NOD, KX, KY, KZ, THS
+      integer(c_int) :: list_s(*)
+      real(c_double) :: list_r(*)
+    end function
+
+    integer(c_int) function qs3g_load_sector(h, NOD, KX, KY, KZ, D, list_s, list_r) bind(C, name="qs3g_load_sector")
+      import :: c_ptr, c_int, c_int64_t, c_double
+      type(c_ptr), value :: h
+      integer(c_int) :: NOD, KX, KY, KZ
+      integer(c_int64_t) :: D
+      integer(c_int64_t) :: list_s(*)
+      real(c_double) :: list_r(*)
+    end function
+
+    ! wall-clock limit of qs3g_trlan, and what the last qs3g_trlan did
+    integer(c_int) function qs3g_set_time_limit(h, seconds) bind(C, name="qs3g_set_time_limit")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: seconds
+    end function
+
+    integer(c_int) function qs3g_trlan_stats(h, hv_fp32, hv_fp64, restarts, seconds, timed_out) &
+        bind(C, name="qs3g_trlan_stats")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: h
+      integer(c_int) :: hv_fp32, hv_fp64, restarts, timed_out
+      real(c_double) :: seconds
+    end function
+
     integer(c_int) function qs3g_get_sector(h, list_s, list_r) bind(C, name="qs3g_get_sector")
       import :: c_ptr, c_int, c_int64_t, c_double
       type(c_ptr), value :: h

@@ -68,9 +68,33 @@ int qs3g_destroy(qs3g_handle h);
 /* Build the (NOD, K) representative basis on the GPU.
  * Replaces allocate_lists_omp_SQ + checkstate_SQ (source/state_lists.f90:66-112,
  * 225-292; called at source/main.f90:54) and the explist of
- * source/input_param.f90:87-89.  D_out receives THS(k). */
+ * source/input_param.f90:87-89.  D_out receives THS(k).
+ * Limits (QS3G_ERANGE beyond them): NOS < 65535; NOD * bits(NOS) <= 64 (one
+ * packed word per row: NOD <= 6 at NOS = 1000); C(NOS, NOD) below 2^63; D
+ * below 2^31; chains (LY = LZ = 1) index the C(NOS-1, NOD-1) configurations
+ * with a down spin on site 1, which must stay below 2^32 (L = 1000 allows
+ * NOD <= 4), other lattices C(NOS, NOD) <= 2^36; the kernels are instantiated
+ * for NOD <= 8 (QS3G_ENOTSUP above). */
 int qs3g_build_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ,
                       int64_t* D_out);
+
+/* The same with the reference's default-kind integer THS
+ * (source/main.f90:28-34): QS3G_ERANGE if the sector has more than
+ * 2^31 - 1 rows or a list_s code above 2^31 - 1 (the reference's own
+ * combination table overflows there). */
+int qs3g_build_sector_i32(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, int* THS);
+
+/* For a caller that already enumerated the sector with allocate_lists_omp_SQ
+ * (source/state_lists.f90:225-292): the (NOD, K) sector is built on the GPU
+ * and compared with the caller's list_s(1:D) (bit for bit) and list_r(1:D)
+ * (1e-12 relative), so the handle's rows are the caller's rows; a mismatch is
+ * QS3G_EINVAL naming the first differing row, and the handle keeps its
+ * previous sector.  The _i32 form takes default-kind THS and list_s
+ * (source/main.f90:28-34, source/ham2vec_v3.f90:45). */
+int qs3g_load_sector(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, const int64_t* D,
+                     const int64_t* list_s, const double* list_r);
+int qs3g_load_sector_i32(qs3g_handle h, const int* NOD, const int* KX, const int* KY, const int* KZ, const int* THS,
+                         const int* list_s, const double* list_r);
 
 /* Build the U(1)-only basis of the variant program: all C(NOS, NOD)
  * configurations, row i = the configuration list_fly(i) of colex rank i, no
@@ -86,6 +110,10 @@ int qs3g_build_sector_u1(qs3g_handle h, const int* NOD, int64_t* D_out);
 /* Copy the sector lists to the host: list_s(1:D) (colex ranks, ascending)
  * and list_r(1:D) = sqrt(norm^2), as allocate_lists_omp_SQ leaves them. */
 int qs3g_get_sector(qs3g_handle h, int64_t* list_s, double* list_r);
+
+/* The same into default-kind integer list_s (QS3G_ERANGE if a code or D
+ * exceeds 2^31 - 1). */
+int qs3g_get_sector_i32(qs3g_handle h, int* list_s, double* list_r);
 
 /* Run the handle's work on a caller-owned CUDA stream (a cudaStream_t passed
  * as void*) instead of the handle's own stream.  No counterpart in the
@@ -163,6 +191,21 @@ int qs3g_trlan(qs3g_handle h, const int* NOE, const int* NOK, const int* NOM, co
                const double* tol, const int* precision, const int* conv_mode,
                const int* start_mode, const uint64_t* seed, const qs3g_cplx* start, double* ene,
                qs3g_cplx* psi, int* iters, double* resid);
+
+/* Wall-clock limit of qs3g_trlan on this handle (seconds; 0 = none, the
+ * default): a solve still running at the limit stops at its next thick
+ * restart and returns QS3G_ENOTCONV with the Ritz pairs it has (a batch job's
+ * time budget; the reference's only limit is maxitr).  No counterpart in the
+ * reference. */
+int qs3g_set_time_limit(qs3g_handle h, const double* seconds);
+
+/* What the last qs3g_trlan call on this handle did: H*v products on
+ * complex(4) and on complex(8) Krylov vectors (the FP64 residual checks
+ * counted with the latter), thick restarts, wall seconds, and 1 in timed_out
+ * if it stopped at the time limit.  Any pointer may be NULL.  The reference
+ * prints its restart count per restart (source/eigen_solver.f90:157-158). */
+int qs3g_trlan_stats(qs3g_handle h, int* hv_fp32, int* hv_fp64, int* restarts, double* seconds,
+                     int* timed_out);
 
 /* Thick-restart Lanczos on n independent problems at once: hs[0..n-1] are
  * handles with built sectors (any lattices, sizes and couplings); each is

@@ -76,6 +76,10 @@ def lib():
         L.ora_connection_table.argtypes = [C.c_void_p, C.c_int, C.c_int64, i64p, C.c_void_p,
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                            C.c_int]
+        L.ora_connection_table_rows.restype = C.c_int64
+        L.ora_connection_table_rows.argtypes = [C.c_void_p, C.c_int, C.c_int64, i64p, C.c_int64,
+                                                C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_int64, C.c_int]
         L.ora_sq_a.restype = C.c_int
         L.ora_sq_a.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int64, i64p, f64p, C.c_int,
                                C.c_int64, i64p, f64p, f64p, f64p, f64p, f64p, f64p, C.c_int]
@@ -205,19 +209,42 @@ class Sector:
                      r0, r1, nthreads)
         return y
 
-    def connection_table(self, nthreads=0):
+    def connection_table(self, nthreads=0, rows=None):
+        """Connection table of ham_to_vec_wave_vector, optionally of rows [r0, r1) only
+        (0-based rows, columns and bonds)."""
         L = lib()
-        nnz = L.ora_connection_table(self.model.h, self.nod, self.D, self.list_s, None, None,
-                                     None, None, 0, nthreads)
+        r0, r1 = (0, self.D) if rows is None else (int(rows[0]), int(rows[1]))
+        nnz = L.ora_connection_table_rows(self.model.h, self.nod, self.D, self.list_s, r0, r1,
+                                          None, None, None, None, 0, nthreads)
+        if nnz < 0:
+            raise ValueError("oracle: bad row range")
         row = np.zeros(nnz, np.int64)
         col = np.zeros(nnz, np.int64)
         ell = np.zeros((nnz, 3), np.int32)
         bond = np.zeros(nnz, np.int32)
-        n2 = L.ora_connection_table(self.model.h, self.nod, self.D, self.list_s, row.ctypes.data,
-                                    col.ctypes.data, ell.ctypes.data, bond.ctypes.data, nnz,
-                                    nthreads)
+        n2 = L.ora_connection_table_rows(self.model.h, self.nod, self.D, self.list_s, r0, r1,
+                                         row.ctypes.data, col.ctypes.data, ell.ctypes.data,
+                                         bond.ctypes.data, nnz, nthreads)
         assert n2 == nnz
         return row, col, ell, bond
+
+    def sparse(self, nthreads=0):
+        """H of the sector as a scipy CSR matrix: one entry per connection-table hop with the
+        coefficient sJint(j,2) * list_r(id) / list_r(i) * explist(ell) of ham2vec_v3.f90:61-65
+        (entries of the same (row, col) summed), plus the diagonal of :60,67 read off one
+        oracle H*v of the all-ones vector.  For solver checks at sizes where dense() is too slow."""
+        import scipy.sparse as sp
+        m = self.model
+        D = self.D
+        row, col, ell, bond = self.connection_table(nthreads)
+        ex1 = m.LX + 1
+        ex2 = ex1 * (m.LY + 1)
+        e = self.explist[ell[:, 0] + ex1 * ell[:, 1] + ex2 * ell[:, 2]]
+        c = (0.5 * m.Jxy[bond]) * self.list_r[col] / self.list_r[row]
+        off = sp.csr_matrix((c * e, (row, col)), shape=(D, D))
+        ones = np.ones(D, np.complex128)
+        diag = (self.hv(ones, nthreads=nthreads) - off @ ones).real
+        return (off + sp.diags(diag)).tocsr()
 
     def dense(self):
         """make_full_hamiltonian (ham2vec_v3.f90:5-35) built column by column through hv."""

@@ -371,19 +371,24 @@ void ora_hv(void* h, int nod, int64_t D, const int64_t* list_s, const double* li
   }
 }
 
-// The connection table of ham_to_vec_wave_vector: one entry (row, col, ell,
-// bond) for every antiparallel bond whose hop lands on a row of the sector
-// (id > 0 in the Fortran), rows ascending, bonds in list order.  Returns nnz,
-// or -1 when cap is too small (pass row == nullptr to count only).
-int64_t ora_connection_table(void* h, int nod, int64_t D, const int64_t* list_s, int64_t* row,
-                             int64_t* col, int* ell3, int* bond, int64_t cap, int nthreads) {
+// The connection table of ham_to_vec_wave_vector restricted to rows
+// [row0, row1): one entry (row, col, ell, bond) for every antiparallel bond
+// whose hop lands on a row of the sector (id > 0 in the Fortran), rows
+// ascending, bonds in list order.  Returns nnz, or -1 when cap is too small
+// (pass row == nullptr to count only).
+int64_t ora_connection_table_rows(void* h, int nod, int64_t D, const int64_t* list_s, int64_t row0,
+                                  int64_t row1, int64_t* row, int64_t* col, int* ell3, int* bond,
+                                  int64_t cap, int nthreads) {
   const Model& m = *(Model*)h;
   int nt = nthreads_or_default(nthreads);
-  std::vector<int64_t> cnt(D + 1, 0);
+  if (row1 > D) row1 = D;
+  if (row0 < 0 || row0 > row1) return -1;
+  const int64_t nr = row1 - row0;
+  std::vector<int64_t> cnt(nr + 1, 0);
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
-  for (int64_t i = 0; i < D; ++i) {
+  for (int64_t r = 0; r < nr; ++r) {
     int st[64], ni[64], ell[3];
-    list_fly(m, list_s[i], nod, st);
+    list_fly(m, list_s[row0 + r], nod, st);
     int64_t c = 0;
     for (int j = 0; j < m.NOxxz; ++j) {
       bool f1 = contains(st, nod, m.p1[j]);
@@ -394,17 +399,18 @@ int64_t ora_connection_table(void* h, int nod, int64_t D, const int64_t* list_s,
         if (findstate(s, list_s, D) >= 0) ++c;
       }
     }
-    cnt[i + 1] = c;
+    cnt[r + 1] = c;
   }
-  for (int64_t i = 0; i < D; ++i) cnt[i + 1] += cnt[i];
-  int64_t nnz = cnt[D];
+  for (int64_t r = 0; r < nr; ++r) cnt[r + 1] += cnt[r];
+  int64_t nnz = cnt[nr];
   if (!row) return nnz;
   if (nnz > cap) return -1;
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
-  for (int64_t i = 0; i < D; ++i) {
+  for (int64_t r = 0; r < nr; ++r) {
+    const int64_t i = row0 + r;
     int st[64], ni[64], ell[3];
     list_fly(m, list_s[i], nod, st);
-    int64_t w = cnt[i];
+    int64_t w = cnt[r];
     for (int j = 0; j < m.NOxxz; ++j) {
       bool f1 = contains(st, nod, m.p1[j]);
       bool f2 = contains(st, nod, m.p2[j]);
@@ -422,6 +428,12 @@ int64_t ora_connection_table(void* h, int nod, int64_t D, const int64_t* list_s,
     }
   }
   return nnz;
+}
+
+// The whole connection table (rows 0..D-1).
+int64_t ora_connection_table(void* h, int nod, int64_t D, const int64_t* list_s, int64_t* row,
+                             int64_t* col, int* ell3, int* bond, int64_t cap, int nthreads) {
+  return ora_connection_table_rows(h, nod, D, list_s, 0, D, row, col, ell3, bond, cap, nthreads);
 }
 
 // Number of connection-table entries (off-diagonal hops that land on a row)
