@@ -65,8 +65,20 @@ void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int
   m.chain = (LY == 1 && LZ == 1);
   m.bits = bits_for(NOS);
   m.p1.resize(NOxxz); m.p2.resize(NOxxz); m.sJxy.resize(NOxxz); m.sJz.resize(NOxxz);
+  // Sz_all and the per-site sums enter every diagonal element; they are
+  // accumulated with compensation (Neumaier), because a running sum of
+  // thousands of equal couplings drifts by up to one rounding per bond
+  // (~1e-11 on a 2000-bond chain) -- the rounding the reference's own
+  // bond-by-bond diagonal carries.
   m.Sz_all = 0.0;
   m.Sz_site.assign(NOS + 1, 0.0);
+  std::vector<double> comp_site(NOS + 1, 0.0);
+  double comp_all = 0.0;
+  auto nsum = [](double& sum, double& comp, double v) {
+    const double t = sum + v;
+    comp += (std::fabs(sum) >= std::fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+  };
   std::vector<std::vector<uint32_t>> adj(NOS + 1);
   for (int b = 0; b < NOxxz; ++b) {
     int a = p_xxz[2 * b], c = p_xxz[2 * b + 1];
@@ -75,14 +87,16 @@ void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int
     m.p1[b] = a; m.p2[b] = c;
     m.sJxy[b] = sJint[b];
     m.sJz[b] = sJint[NOxxz + b];
-    m.Sz_all += m.sJz[b];
+    nsum(m.Sz_all, comp_all, m.sJz[b]);
     if (a != c) {
       adj[a].push_back(((uint32_t)b << 16) | (uint32_t)c);
       adj[c].push_back(((uint32_t)b << 16) | (uint32_t)a);
-      m.Sz_site[a] += m.sJz[b];
-      m.Sz_site[c] += m.sJz[b];
+      nsum(m.Sz_site[a], comp_site[a], m.sJz[b]);
+      nsum(m.Sz_site[c], comp_site[c], m.sJz[b]);
     }
   }
+  m.Sz_all += comp_all;
+  for (int i = 0; i <= NOS; ++i) m.Sz_site[i] += comp_site[i];
   m.adj_off.assign(NOS + 2, 0);
   m.adj.clear();
   for (int s = 1; s <= NOS; ++s) {

@@ -925,6 +925,16 @@ double est_factor() {
   return v;
 }
 
+// Precision 1 with NOE = 1 runs the anchored solver (trlan_anchor.cu) unless
+// QS3G_ANCHOR=0.
+bool anchored_enabled() {
+  static const bool v = [] {
+    const char* e = std::getenv("QS3G_ANCHOR");
+    return !(e && e[0] == '0');
+  }();
+  return v;
+}
+
 // QS3G_VERBOSE=1 prints one progress line per restart, as QS3 does.
 bool verbose() {
   static const bool v = [] {
@@ -1167,7 +1177,33 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
   }
   bool converged = false;
   DevBuf<double2> V64((size_t)ldv * (NOM + 1)), Q64(D);
-  if (p.precision == 1) {
+  // Precision 1 for the lowest eigenpair: the anchored solver keeps the
+  // approximation in FP64 and every Krylov vector in FP32 to the end; if its
+  // residual stalls (an FP32 floor), the double-float attempts below continue
+  // from its vector.  QS3G_ANCHOR=0 selects the two-phase form instead.
+  bool anchored = false, anchored_done = false, anchored_conv = false;
+  int hv_fp32 = 0;
+  if (p.precision == 1 && NOE == 1 && anchored_enabled()) {
+    anchored = true;
+    Ops<double2> o64{st, sc.part.get()};
+    if (start64) QS3G_CHECK_CUDA(cudaMemcpyAsync(V64.get(), start64, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    else o64.random_start(V64.get(), n, p.seed);
+    if (real && (D & 1)) QS3G_CHECK_CUDA(cudaMemsetAsync(reinterpret_cast<double*>(V64.get()) + D, 0, sizeof(double), st));
+    AnchorParams ap;
+    ap.NOK = NOK; ap.NOM = NOM; ap.maxitr = p.maxitr; ap.conv_mode = p.conv_mode; ap.tol = p.tol;
+    ap.real = real; ap.n = n; ap.ldv = ldv; ap.deadline = deadline;
+    const AnchorOut a = trlan_anchored(m, s, ap, V64.get(), st);
+    hv_fp32 = a.hv32;
+    hv_total += a.hv32 + a.hv64;
+    restarts_total += a.restarts;
+    timed_out = a.timed_out;
+    ene_phase1.assign(1, a.ene);
+    anchored_done = !a.stalled;
+    anchored_conv = a.converged;
+    if (verbose())
+      std::printf("trlan: anchored solve %s after %d cycles, ||r|| = %.3e\n",
+                  a.converged ? "converged" : (a.stalled ? "stalled" : "stopped"), a.restarts, a.resid);
+  } else if (p.precision == 1) {
     // phase 1: complex(4) Krylov storage, FP64 reductions and Ritz solve
     DevBuf<float2> V32((size_t)ldv * (NOM + 1)), Q32(n);
     Ops<float2> o32{st, sc.part.get()};
@@ -1183,6 +1219,7 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     restarts_total += r1.restarts;
     timed_out = r1.timed_out;
     ene_phase1 = r1.ene;
+    hv_fp32 = r1.hv_count;
     // phase 2: FP64 thick-restart Lanczos from the sum of the NOE Ritz vectors
     Ops<double2> o64{st, sc.part.get()};
     f32_to_f64(V64.get(), V32.get(), n, st);
@@ -1198,7 +1235,7 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     else o64.random_start(V64.get(), n, p.seed);
     if (real && (D & 1)) QS3G_CHECK_CUDA(cudaMemsetAsync(reinterpret_cast<double*>(V64.get()) + D, 0, sizeof(double), st));
   }
-  const int hv_phase1 = hv_total;
+  const int hv_phase1 = hv_fp32;
   // With a residual target (conv_mode 1, 2) the Ritz estimate |beta C| can sit
   // below the true residual; the run is accepted only when the FP64 residual
   // ||H psi - E psi|| recomputed from the Ritz vectors meets the target, else it
@@ -1234,7 +1271,11 @@ int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* 
     };
   }
   TrlanOut r2;
-  for (int attempt = 0; attempt < 4 && !timed_out; ++attempt) {
+  if (anchored_done) {
+    r2.ene = ene_phase1;
+    r2.converged = anchored_conv;
+  }
+  for (int attempt = 0; attempt < 4 && !timed_out && !anchored_done; ++attempt) {
     const bool eft = p.precision != 0 && attempt < 2;
     if (attempt == 0) {
       r2 = trlan_core<double2>(m, s, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est, p.conv_mode, st,

@@ -99,6 +99,25 @@ struct TrlanParams {
 int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<const Sector*>& secs,
                    const TrlanParams& p, double* ene, double* resid, int* hv, int* status, cudaStream_t st);
 
+// Thick-restart Lanczos for the lowest eigenpair on FP32 Krylov vectors
+// anchored on one FP64 vector (trlan_anchor.cu).  x: the FP64 start vector
+// on entry (n slots, leading dimension ldv for the FP32 basis), the
+// normalised Ritz vector on return.
+struct AnchorParams {
+  int NOK = 16, NOM = 48, maxitr = 1000, conv_mode = 1;
+  double tol = 1e-10;
+  bool real = false;
+  int64_t n = 0, ldv = 0;
+  double deadline = 0.0;   // steady-clock seconds; 0: none
+  int stall_cycles = 40;   // cycles without a 10 % residual drop before giving up
+};
+struct AnchorOut {
+  double ene = 0.0, resid = 0.0;  // Rayleigh quotient and FP64 residual of x
+  int hv32 = 0, hv64 = 0, restarts = 0;
+  bool converged = false, stalled = false, timed_out = false;
+};
+AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p, double2* x, cudaStream_t st);
+
 int trlan(const Model& m, const Sector& s, const TrlanParams& p, const double2* h_start, double* ene_out,
           double2* h_psi, int* iters, double* resid, cudaStream_t st, TrlanStats* stats = nullptr);
 int lanczos(const Model& m, const Sector& s, int maxitr, int minitr, int itrint, double tol, const double2* h_start,
