@@ -136,6 +136,31 @@ __device__ __forceinline__ float2 row_out(float di, float2 xi, float ax, float a
 __device__ __forceinline__ double row_out(double di, double xi, double ax, double) { return fma(di, xi, ax); }
 __device__ __forceinline__ float row_out(float di, float xi, float ax, float) { return fmaf(di, xi, ax); }
 
+// The general hop: j_flip_ni + representative_SQ on the sorted configuration
+// (move_spin, then the gap-key search of chain_rep_count).  Returns the row id
+// (or -1), the translation ell and the target's self-translation count.
+template <int NOD>
+__device__ __forceinline__ int chain_hop_general(const HvArgs& a, const int (&n)[NOD], int m, int e, int& ell,
+                                                 int& cnt) {
+  int o[NOD], p[NOD];
+  move_spin<NOD>(n, m, e, o);
+  chain_rep_count<NOD>(o, a.L, a.bits, p, ell, cnt);
+  return dir_lookup32(a.dir, anchored_index32<NOD>(p, a.binomA, a.L));
+}
+
+// Chain rows work on the cyclic gaps g[k] = n[k+1] - n[k] (lane k; lane NOD-1
+// wraps).  A hop moves spin m by del = e - n[m] (taken the short way round the
+// ring); when it neither lands on nor passes another spin (|del| below the gap
+// on its side) only lanes m-1 and m change, by +del and -del.  The
+// representative is then read off the lanes directly: with a unique largest
+// gap at lane c, the spin after it (c+1) goes to site 1, the representative's
+// sites are 1, 1 + g[c+1], 1 + g[c+1] + g[c+2], ... (the last one 1 + L -
+// g[c]), it has one self-translation, and representative_SQ's ell is
+// L - site + 1 of that spin (0 when it already sits on site 1).  The
+// anchored index sum_{j>=1} C(p_j - 2, j) and the directory give the row --
+// the same (id, ell, count) as the general path, so the products are
+// bit-identical.  Moves onto or past another spin, tied largest gaps and a
+// single down spin take the general path.
 template <int NOD, bool KZERO, class V>
 __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
                                              const double* __restrict__ diag,
@@ -145,24 +170,78 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   using R = typename Cplx<V>::R;
   int n[NOD];
   unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  int g[NOD];
+#pragma unroll
+  for (int k = 0; k < NOD - 1; ++k) g[k] = n[k + 1] - n[k];
+  g[NOD - 1] = n[0] + a.L - n[NOD - 1];
   const V xi = x[i];
   const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
+  const int L = a.L, half = a.L >> 1;
   R ax = 0, ay = 0;
 #pragma unroll
   for (int m = 0; m < NOD; ++m) {
     const int d = n[m];
+    const int mp = (m + NOD - 1) % NOD;  // lane before spin m
+    const int gn = g[m], gp = g[mp];
+    // the largest of the other lanes, its lane and how often it occurs
+    int omax = -1, oarg = 0, oties = 0;
+#pragma unroll
+    for (int k = 0; k < NOD; ++k) {
+      if (k == m || k == mp) continue;
+      oties = (g[k] == omax) ? oties + 1 : ((g[k] > omax) ? 1 : oties);
+      oarg = (g[k] > omax) ? k : oarg;
+      omax = max(omax, g[k]);
+    }
     const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
     for (int t = e0; t < e1; ++t) {
       const uint32_t w = __ldg(a.adj + t);
       const int e = (int)(w & 0xffffu);
-      bool edown = false;
+      int del = e - d;
+      del += (del > half) ? -L : ((del < -half) ? L : 0);
+      const int ad = del > 0 ? del : -del;
+      int id, ell = 0, cnt = 1;
+      int lm = 0, ln = 0, mx = 0, c = 0, nmx = 0;
+      if (NOD >= 2) {
+        lm = gp + del;  // new lane m-1
+        ln = gn - del;  // new lane m
+        mx = max(max(lm, ln), omax);
+        nmx = (lm == mx) + (ln == mx) + (omax == mx ? oties : 0);
+        c = (lm == mx) ? mp : ((ln == mx) ? m : oarg);
+      }
+      if (NOD >= 2 && ad < (del > 0 ? gn : gp) && nmx == 1) {
+        // lanes c+1, c+2, ... of the moved configuration, as sites p_1, p_2, ...
+        uint32_t idx = 0;
+        int pj = 1;
 #pragma unroll
-      for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
-      if (edown) continue;  // parallel bond: diagonal only
-      int o[NOD], p[NOD], ell, cnt;
-      move_spin<NOD>(n, m, e, o);
-      chain_rep_count<NOD>(o, a.L, a.bits, p, ell, cnt);
-      const int id = dir_lookup32(a.dir, anchored_index32<NOD>(p, a.binomA, a.L));
+        for (int j = 1; j < NOD; ++j) {
+          int lane = 0;
+#pragma unroll
+          for (int k = 0; k < NOD; ++k) {
+            const int vk = (k == mp) ? lm : ((k == m) ? ln : g[k]);
+            lane = (c == (k - j + NOD) % NOD) ? vk : lane;
+          }
+          pj += lane;
+          const uint32_t xj = (uint32_t)(pj - 2);
+          if (j == 1) idx += xj;
+          else if (j == 2) idx += (xj * (xj - 1u)) >> 1;
+          else idx += __ldg(a.binomA + (size_t)(j - 1) * (L - 1) + xj);
+        }
+        id = dir_lookup32(a.dir, idx);
+        if constexpr (!KZERO) {
+          const int sw = (c + 1) % NOD;  // the spin that goes to site 1
+          int site = n[0];
+#pragma unroll
+          for (int k = 1; k < NOD; ++k) site = (sw == k) ? n[k] : site;
+          site = (sw == m) ? e : site;
+          ell = (site == 1) ? 0 : L - site + 1;
+        }
+      } else {
+        bool edown = false;
+#pragma unroll
+        for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+        if (edown) continue;  // parallel bond: diagonal only
+        id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+      }
       if (id < 0) continue;
       V xv = x[id];
       if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);

@@ -109,7 +109,7 @@ struct AnchorParams {
   bool real = false;
   int64_t n = 0, ldv = 0;
   double deadline = 0.0;   // steady-clock seconds; 0: none
-  int stall_cycles = 40;   // cycles without a 10 % residual drop before giving up
+  int stall_cycles = 30;   // cycles with neither a lower energy nor a 10 % residual drop before handing over
 };
 struct AnchorOut {
   double ene = 0.0, resid = 0.0;  // Rayleigh quotient and FP64 residual of x

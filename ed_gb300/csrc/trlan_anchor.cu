@@ -307,7 +307,8 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   QS3G_REQUIRE(NOK >= 1 && NOM >= NOK + 2 && NOM <= 120, QS3G_EINVAL, "anchored Lanczos needs NOK + 2 <= NOM <= 120");
   const bool real = p.real;
   const int64_t n = p.n, ldv = p.ldv;
-  const double sigma = m.Sz_all;
+  // the FP32 products apply H - fl32(sigma); every FP64 quantity uses the same shift
+  const double sigma = (double)(float)m.Sz_all;
   AnchorOut out;
   DevBuf<float2> W((size_t)ldv * (NOM + 1));
   DevBuf<double2> hx(n), hs(n), r(n), xn(n);
@@ -361,7 +362,7 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   o64.scale_inv(x, n, d_rn);
   int ky = 0;
   std::vector<double> thY;  // Ritz values of the retained vectors, on H - sigma
-  double best = 1e300, prev_theta = 0.0;
+  double best = 1e300, best_theta = 1e300, prev_theta = 0.0;
   int stall = 0, flag = 0;
   const int NB = NOM + 1;
   std::vector<double2> h_all;
@@ -398,8 +399,19 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
       out.converged = true;
       break;
     }
-    if (rn < 0.9 * best) { best = rn; stall = 0; }
-    else if (++stall >= p.stall_cycles) { out.stalled = true; break; }
+    // Progress is a lower Rayleigh quotient or a smaller residual.  Thick-restart
+    // Lanczos passes plateaus where the residual rises for many cycles while a
+    // near-degenerate competitor is resolved (the energy keeps falling then);
+    // only when neither moves is the FP32 basis at its floor.
+    const bool lower = theta < best_theta - 1e-15 * std::max(1.0, std::fabs(theta));
+    if (rn < 0.9 * best || lower) {
+      stall = 0;
+      best = std::min(best, rn);
+      best_theta = std::min(best_theta, theta);
+    } else if (++stall >= p.stall_cycles) {
+      out.stalled = true;
+      break;
+    }
     if (cyc == p.maxitr) break;
     if (p.deadline > 0.0 && now_s() > p.deadline) { out.timed_out = true; break; }
     // 2. x's row of G and M against the retained vectors; the extension start

@@ -356,3 +356,33 @@ def test_general_hv_schedules_identical(qs3g, LX, LY, LZ, nod, K, kind):
     np.testing.assert_array_equal(h.hv32(x32), out[1][1])
     assert h.hv_schedule()[0] in (1, 2) and h.hv_schedule()[1] in (1, 2)
     h.close()
+
+
+@pytest.mark.parametrize("L,nod,K,offsets", [(20, 4, 3, (1, 3, 4)), (18, 5, 0, (1, 2, 5)), (16, 3, 5, (2, 7)),
+                                             (24, 2, 0, (1, 12)), (15, 6, 4, (1, 2, 3))])
+def test_chain_long_range_bonds(qs3g, L, nod, K, offsets):
+    """Chains whose bonds reach several sites: hops that pass over other down
+    spins, land next to them or wrap round the ring take the general path, the
+    rest the gap-lane path; both must give the oracle's connection table and
+    H*v (complex(8), complex(4) and, at K = 0, real)."""
+    rng = np.random.default_rng(L * 10 + nod)
+    bonds = [(s, (s - 1 + o) % L + 1) for o in offsets for s in range(1, L + 1)]
+    if L % 2 == 0 and L // 2 in offsets:  # the half-ring bond appears twice; keep one copy per pair
+        seen, uniq = set(), []
+        for a, b in bonds:
+            key = (min(a, b), max(a, b))
+            if key not in seen:
+                seen.add(key)
+                uniq.append((a, b))
+        bonds = uniq
+    bonds = np.array(bonds, np.int32)
+    jxy = rng.uniform(0.5, 1.5, len(bonds))
+    jz = rng.uniform(-1.0, 1.0, len(bonds))
+    om, osec, h, D = both((L, L, 1, 1, bonds, jxy, jz), nod, (K, 0, 0))
+    check_sector(osec, h, D)
+    check_table(osec, h)
+    check_hv(osec, h, seed=L)
+    if K == 0:
+        x = rng.standard_normal(D)
+        np.testing.assert_array_equal(h.hv_real(x), h.hv(x.astype(np.complex128)).real)
+    h.close()
