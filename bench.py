@@ -336,6 +336,41 @@ def cpu_leg(args, h, x, y, D):
     return cpu, parity
 
 
+ARMS = {  # name: (qs3g_trlan precision, learned start)
+    "learned_fp32_real": (1 | 8, True), "learned_fp32": (1, True), "random_fp32_real": (1 | 8, False),
+    "random_fp32": (1, False), "random_fp64_real": (0 | 8, False), "random_df": (2, False),
+    "plain_fp64_random": (0, False),
+}
+
+
+def solve_arm(args):
+    """One arm of the ground-state solve alone (--arm NAME), stopped after
+    --arm-limit seconds: for profiling the solver on the benchmark chain."""
+    from ed_gb300 import capi, learned
+    prec, use_net = ARMS[args.arm]
+    delta, j2 = J1[1], J2[0]
+    v = None
+    h = learned.chain_handle(args.L, delta, j2)
+    if use_net:
+        net = capi.Mlp(seed=1)
+        learned.generate(net, learned.training_problems(seed=1))
+        learned.train(net, rounds=10, steps=300, batch=4096, lr=2e-3)
+    D = h.build_sector(NOD, (0, 0, 0))
+    if use_net:
+        v = learned.start_vector(net, h, delta, j2)
+    h.set_time_limit(args.arm_limit)
+    t0 = time.perf_counter()
+    r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec, conv_mode=1, seed=7,
+                start=v, want_psi=False, allow_unconverged=True)
+    dt = time.perf_counter() - t0
+    st = h.trlan_stats()
+    h.close()
+    print(json.dumps({"arm": args.arm, "L": args.L, "sector_dim": D, "seconds": dt, "E0": float(r["ene"][0]),
+                      "resid": float(r["resid"][0]), "converged": bool(r["converged"]), "hv": r["iters"],
+                      "hv_fp32": st["hv_fp32"], "hv_fp64": st["hv_fp64"], "restarts": st["restarts"],
+                      "timed_out": st["timed_out"]}), flush=True)
+
+
 def solve_bench(args):
     """Ground state of the benchmark chain (L, N_down=4, k=0, Delta=0.5, J2=0.3,
     an unseen point of the network's training range) to ||H psi - E psi|| <= tol,
@@ -343,9 +378,9 @@ def solve_bench(args):
 
       learned_fp32_real  the network's start vector (trained here on chains
                          L = 48..128 whose ground states the GPU TRLan computes
-                         first), complex(4) Krylov storage with FP64-accurate
-                         reductions and refinement, real vectors (k = 0: H is
-                         real symmetric);
+                         first), precision 1: every Krylov vector in FP32,
+                         anchored on one FP64 vector, FP64-accurate reductions,
+                         real vectors (k = 0: H is real symmetric);
       plain_fp64_random  the reference's arithmetic: complex(8) vectors, FP64
                          throughout, random start (eigen_solver.f90:92-96),
                          stopped at plain_limit seconds if it has not converged.
@@ -464,6 +499,9 @@ def main():
     ap.add_argument("--nom", type=int, default=48)
     ap.add_argument("--maxrestart", type=int, default=40000)
     ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--arm", choices=sorted(ARMS), default=None,
+                    help="run only this arm of the ground-state solve (no H*v leg) and print its line")
+    ap.add_argument("--arm-limit", type=float, default=0.0, help="wall seconds for --arm (0: none)")
     ap.add_argument("--plain-limit", type=float, default=1200.0,
                     help="wall seconds after which the plain FP64 solve stops (reported as a lower bound)")
     ap.add_argument("--L", type=int, default=1000,
@@ -477,7 +515,11 @@ def main():
         args.warmup = 3
     rank, world, local_rank, dist = dist_setup()
     try:
-        if args.impl == "reference":
+        if args.arm and rank == 0:
+            solve_arm(args)
+        elif args.arm:
+            pass
+        elif args.impl == "reference":
             run_reference(args, rank, world, dist)
         else:
             run_gpu(args, rank, world, local_rank, dist)
