@@ -271,6 +271,7 @@ def run_gpu(args, rank, world, local_rank, dist):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    line["hv_variants"] = hv_variants(h, x, D, stream, dev)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"], line["parity"] = cpu_leg(args, h, x, y, D)
     h.close()
@@ -280,6 +281,38 @@ def run_gpu(args, rank, world, local_rank, dist):
         line["dsf_batch"] = dsf_bench()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def hv_variants(h, x, D, stream, dev, reps=10):
+    """CUDA-event time of the other forms of the same product on the same sector
+    (real vectors: k = 0, H real symmetric): real FP64, complex(4) and real
+    FP32, each with its algorithmic bytes D*(2 s + 16) + nnz_off*(s + 8)."""
+    import torch
+    from ed_gb300 import capi
+    nnz = int(h.connection_table_count())
+    out = {}
+    xr = x.real.contiguous()
+    x32 = x.to(torch.complex64)
+    xr32 = xr.to(torch.float32)
+    forms = [("real_f64", lambda a, b: h.hv_real_device(a, b), xr, 8),
+             ("complex_f32", lambda a, b: h.hv32_device(a, b), x32, 8),
+             ("real_f32", lambda a, b: h.hv32_real_device(a, b), xr32, 4)]
+    for name, fn, xv, s in forms:
+        yv = torch.empty_like(xv)
+        for _ in range(3):
+            fn(xv.data_ptr(), yv.data_ptr())
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        for _ in range(reps):
+            fn(xv.data_ptr(), yv.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = ev0.elapsed_time(ev1) / reps
+        B = D * (2 * s + 16) + nnz * (s + 8)
+        out[name] = {"ms": ms, "algorithmic_gbs": B / (ms * 1e-3) / 1e9}
+        del yv
+    return out
 
 
 def cpu_leg(args, h, x, y, D):

@@ -37,6 +37,7 @@ EXPORTS = [
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
     "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real", "qs3g_set_time_limit", "qs3g_trlan_stats",
     "qs3g_build_sector_i32", "qs3g_get_sector_i32", "qs3g_load_sector", "qs3g_load_sector_i32",
+    "qs3g_hv32_real",
 ]
 
 MLP_NPARAMS = 35329
@@ -227,6 +228,19 @@ class Handle:
         y = np.zeros(self.D, np.float64)
         _check(load().qs3g_hv_real(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
         return y
+
+    def hv32_real(self, x, shift=0.0):
+        """y = (H - shift) x in FP32 for a real vector x (sectors whose H is real symmetric)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        assert x.shape == (self.D,)
+        y = np.zeros(self.D, np.float32)
+        sh = C.c_float(float(shift))
+        _check(load().qs3g_hv32_real(self.h, _ptr(y), _ptr(x), C.byref(sh), _i(HOST)), self.h)
+        return y
+
+    def hv32_real_device(self, x_ptr: int, y_ptr: int, shift=0.0):
+        sh = C.c_float(float(shift))
+        _check(load().qs3g_hv32_real(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), C.byref(sh), _i(DEVICE)), self.h)
 
     def hv_real_device(self, x_ptr: int, y_ptr: int):
         _check(load().qs3g_hv_real(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)

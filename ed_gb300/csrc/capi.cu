@@ -377,6 +377,28 @@ int qs3g_hv_real(qs3g_handle h, double* v0, const double* v1, const int* where) 
   });
 }
 
+int qs3g_hv32_real(qs3g_handle h, float* v0, const float* v1, const float* shift, const int* where) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(v0 && v1 && where, QS3G_EINVAL, "null argument");
+    QS3G_REQUIRE(real_sector(s), QS3G_ENOTSUP, "real H*v needs a k = 0 chain sector or a U(1) sector");
+    const float sh = shift ? *shift : 0.f;
+    if (*where == QS3G_DEVICE) {  // asynchronous on the handle's stream
+      hv32r(h->model, s, v1, v0, h->stream, sh, false);
+      return QS3G_OK;
+    }
+    QS3G_REQUIRE(*where == QS3G_HOST, QS3G_EINVAL, "where must be QS3G_HOST or QS3G_DEVICE");
+    const size_t bytes = (size_t)s.D * sizeof(float);
+    auto* x = static_cast<float*>(staging(h, 0, bytes));
+    auto* y = static_cast<float*>(staging(h, 1, bytes));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(x, v1, bytes, cudaMemcpyHostToDevice, h->stream));
+    hv32r(h->model, s, x, y, h->stream, sh, false);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v0, y, bytes, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
 int qs3g_set_stream(qs3g_handle h, void* stream) {
   return guarded(h, [&]() {
     QS3G_REQUIRE(h, QS3G_EINVAL, "null handle");

@@ -178,6 +178,7 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
   const int L = a.L, half = a.L >> 1;
   R ax = 0, ay = 0;
+  uint64_t deferred = 0;  // bit 8 m + s: bond s (< 8) of spin m takes the general path
 #pragma unroll
   for (int m = 0; m < NOD; ++m) {
     const int d = n[m];
@@ -209,22 +210,37 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
         c = (lm == mx) ? mp : ((ln == mx) ? m : oarg);
       }
       if (NOD >= 2 && ad < (del > 0 ? gn : gp) && nmx == 1) {
-        // lanes c+1, c+2, ... of the moved configuration, as sites p_1, p_2, ...
+        // lanes c+1, c+2, ... of the moved configuration, as sites p_1, p_2, ...;
+        // the last site is always 1 + L - (largest gap)
         uint32_t idx = 0;
-        int pj = 1;
+        if constexpr (NOD == 4) {
+          // the four cases of c: lane m-1, lane m, or the larger other lane
+          const int m1 = (m + 1) % NOD, m2 = (m + 2) % NOD;
+          const bool cA = (lm == mx), cB = (ln == mx), o1 = (oarg == m1);
+          const int G1 = cA ? ln : (cB ? g[m1] : (o1 ? g[m2] : lm));
+          const int G12 = cA ? ln + g[m1] : (cB ? g[m1] + g[m2] : (o1 ? g[m2] + lm : lm + ln));
+          const uint32_t x2 = (uint32_t)(G12 - 1);
+          idx = (uint32_t)(G1 - 1) + ((x2 * (x2 - 1u)) >> 1) + __ldg(a.binomA + 2 * (size_t)(L - 1) + (L - 1 - mx));
+        } else {
+          int pj = 1;
 #pragma unroll
-        for (int j = 1; j < NOD; ++j) {
-          int lane = 0;
+          for (int j = 1; j < NOD; ++j) {
+            int lane = 0;
+            if (j == NOD - 1) {
+              lane = L - mx - (pj - 1);
+            } else {
 #pragma unroll
-          for (int k = 0; k < NOD; ++k) {
-            const int vk = (k == mp) ? lm : ((k == m) ? ln : g[k]);
-            lane = (c == (k - j + NOD) % NOD) ? vk : lane;
+              for (int k = 0; k < NOD; ++k) {
+                const int vk = (k == mp) ? lm : ((k == m) ? ln : g[k]);
+                lane = (c == (k - j + NOD) % NOD) ? vk : lane;
+              }
+            }
+            pj += lane;
+            const uint32_t xj = (uint32_t)(pj - 2);
+            if (j == 1) idx += xj;
+            else if (j == 2) idx += (xj * (xj - 1u)) >> 1;
+            else idx += __ldg(a.binomA + (size_t)(j - 1) * (L - 1) + xj);
           }
-          pj += lane;
-          const uint32_t xj = (uint32_t)(pj - 2);
-          if (j == 1) idx += xj;
-          else if (j == 2) idx += (xj * (xj - 1u)) >> 1;
-          else idx += __ldg(a.binomA + (size_t)(j - 1) * (L - 1) + xj);
         }
         id = dir_lookup32(a.dir, idx);
         if constexpr (!KZERO) {
@@ -236,6 +252,15 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
           ell = (site == 1) ? 0 : L - site + 1;
         }
       } else {
+        // onto / past another spin, or a tie: the general path, after the loop
+        // (the lanes of a warp that need it then share one pass instead of
+        // stalling the others at every hop); bonds past the 8th of a site
+        // take it inline
+        const int slot = t - e0;
+        if (slot < 8) {
+          deferred |= 1ull << (8 * m + slot);
+          continue;
+        }
         bool edown = false;
 #pragma unroll
         for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
@@ -247,6 +272,26 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
       if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
       hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
     }
+  }
+  while (deferred) {
+    const int b = __ffsll((long long)deferred) - 1;
+    deferred &= deferred - 1;
+    const int m = b >> 3;
+    int d = n[0];
+#pragma unroll
+    for (int k = 1; k < NOD; ++k) d = (m == k) ? n[k] : d;
+    const uint32_t w = __ldg(a.adj + __ldg(a.adj_off + d) + (b & 7));
+    const int e = (int)(w & 0xffffu);
+    bool edown = false;
+#pragma unroll
+    for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+    if (edown) continue;  // parallel bond: diagonal only
+    int ell = 0, cnt = 1;
+    const int id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+    if (id < 0) continue;
+    V xv = x[id];
+    if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+    hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
   }
   const R ir = __ldg(invR + chain_self_count<NOD>(n, a.L, a.bits));
   y[i] = row_out(di, xi, ir, ax, ay);

@@ -5,8 +5,8 @@
 //
 // Network: x (16 inputs) -> 128 -> 128 -> 128 -> 1, tanh hidden activations.
 // Parameters are kept in FP32 (master, Adam moments) and used rounded to
-// BF16; inputs are rounded to BF16; every product is accumulated in FP32 and
-// hidden activations stay FP32.  Inputs for rotation s of a representative
+// BF16; inputs, hidden activations and back-propagated signals are BF16;
+// every product is accumulated in FP32.  Inputs for rotation s of a representative
 // with sorted sites n_0 < ... < n_{N-1} (N = NOD <= 4) on a ring of L sites:
 //   gaps g_j = n_{j+1} - n_j, g_{N-1} = n_0 + L - n_{N-1};  h_j = g_{(s+j) mod N}
 //   x = [h_j / L (j < N), cos(q0 h_j) (j < N), sin(q0 h_j) (j < N), Delta, J2, 0...]
@@ -16,15 +16,19 @@
 //   f(r) ~ psi(config r) * sqrt(C(L, N)),  start vector v_r = f(r) * L / list_r(r)
 // (for k = 0 the basis state of representative r is sum_t T^t|r> / list_r(r)).
 //
-// Kernels (hand-written, SIMT, no tensor cores: the network is small and
-// this is not the solver's hot path):
+// Kernels (hand-written; every matrix product on the tensor cores as
+// mma.sync m16n8k16 BF16 x BF16 -> FP32):
 //   k_mlp_forward  one tile = 64 rows (16 representatives x 4 rotations); BF16
-//                  weights staged in shared memory, activations transposed
-//                  [feature][row] in FP32; each thread owns a 4-row x 8-column
-//                  register block of every layer's output.
+//                  weights staged transposed in shared memory, activations
+//                  row-major BF16 tiles; each warp computes a 16 x 64 block of
+//                  a layer's output, bias + tanh in the epilogue.
 //   k_mlp_train    the same forward plus the backward pass for a batch of
-//                  representatives, gradients accumulated into a per-block
-//                  partial (each block owns its slice: no atomics), loss in FP64.
+//                  representatives: weight gradients IN^T DZ and data gradients
+//                  DZ W^T on the tensor cores (operands transposed on the fly
+//                  by ldmatrix.trans), the back-propagated signals rounded to
+//                  BF16 like the activations; gradients accumulated into a
+//                  per-block partial (each block owns its slice: no atomics),
+//                  loss in FP64.
 //   k_mlp_reduce   fixed-order sum of the per-block partials (deterministic).
 //   k_mlp_adam     Adam step on the FP32 master copy, refresh of the BF16 copy.
 #include <cuda_bf16.h>
@@ -43,28 +47,33 @@ namespace qs3g {
 namespace {
 
 constexpr int kIn = kMlpIn, kHid = kMlpHid;
-constexpr int kTile = 64;          // rows per tile
-constexpr int kThreads = 256;
-constexpr int kWP = 130;           // BF16 weight pitch (65 words: column reads hit 32 banks)
-constexpr int kAP = 68;            // FP32 activation pitch [feature][row]
+constexpr int kTile = 64;          // rows per tile (16 representatives x 4 rotations)
+constexpr int kThreads = 256;      // 8 warps
+constexpr int kXP = kIn + 8;       // BF16 pitch of the input tile and of W1^T (24 elements, 48 bytes)
+constexpr int kHP = kHid + 8;      // BF16 pitch of the activation tiles and of W2^T, W3^T (136, 272 bytes)
 
 constexpr int kOffW1 = kMlpOffW1, kOffB1 = kMlpOffB1, kOffW2 = kMlpOffW2, kOffB2 = kMlpOffB2, kOffW3 = kMlpOffW3,
               kOffB3 = kMlpOffB3, kOffW4 = kMlpOffW4, kOffB4 = kMlpOffB4, kNP = kMlpNParams;
 
-// shared-memory layout (bytes)
-constexpr size_t kSmW1 = 0;
-constexpr size_t kSmW2 = kSmW1 + (size_t)kIn * kWP * 2;
-constexpr size_t kSmW3 = kSmW2 + (size_t)kHid * kWP * 2;
-constexpr size_t kSmVec = kSmW3 + (size_t)kHid * kWP * 2;          // b1 b2 b3 w4 b4 (FP32)
-constexpr size_t kSmX = kSmVec + (size_t)(4 * kHid + 4) * 4;
-constexpr size_t kSmH1 = kSmX + (size_t)kIn * kAP * 4;
-constexpr size_t kSmH2 = kSmH1 + (size_t)kHid * kAP * 4;
-constexpr size_t kSmH3 = kSmH2 + (size_t)kHid * kAP * 4;
-constexpr size_t kSmG = kSmH3 + (size_t)kHid * kAP * 4;
-constexpr size_t kSmRow = kSmG + (size_t)kHid * kAP * 4;             // out[64], dout[64]
+// Shared-memory layout (bytes).  Every region and every row starts on a
+// 16-byte boundary (ldmatrix rows); the pitches put the 8 rows a fragment
+// load touches on 8 different bank quads, so no access conflicts.
+constexpr size_t kSmW1 = 0;                                        // W1^T [128][24]  (BF16)
+constexpr size_t kSmW2 = kSmW1 + (size_t)kHid * kXP * 2;           // W2^T [128][136]
+constexpr size_t kSmW3 = kSmW2 + (size_t)kHid * kHP * 2;           // W3^T [128][136]
+constexpr size_t kSmVec = kSmW3 + (size_t)kHid * kHP * 2;          // b1 b2 b3 w4 b4 (FP32)
+constexpr size_t kSmX = kSmVec + (size_t)(4 * kHid + 4) * 4;       // X  [64][24]    (BF16)
+constexpr size_t kSmH1 = kSmX + (size_t)kTile * kXP * 2;           // H1 [64][136]   (BF16)
+constexpr size_t kSmH2 = kSmH1 + (size_t)kTile * kHP * 2;          // H2
+constexpr size_t kSmH3 = kSmH2 + (size_t)kTile * kHP * 2;          // H3 (training; inference: out[64])
+constexpr size_t kSmG = kSmH3 + (size_t)kTile * kHP * 2;           // dz [64][136]   (BF16)
+constexpr size_t kSmRow = kSmG + (size_t)kTile * kHP * 2;          // out[64], dout[64] (FP32)
 constexpr size_t kSmTrain = kSmRow + 2 * kTile * 4;
-constexpr size_t kSmInfer = kSmH3;                                   // x, h1, h2 only (+ row)
+constexpr size_t kSmInfer = kSmH3 + kTile * 4;
 static_assert(kSmTrain <= 232448, "training tile exceeds shared memory");
+static_assert(kSmX % 16 == 0 && kSmH1 % 16 == 0 && kSmW2 % 16 == 0 && kSmG % 16 == 0, "16-byte regions");
+
+using bf16 = __nv_bfloat16;
 
 struct MlpArgs {
   const uint64_t* conf;       // packed representative per rep
@@ -75,7 +84,7 @@ struct MlpArgs {
   int64_t nreps;              // reps addressed by this launch
   const int64_t* index;       // training: rep index per batch entry (null: identity)
   const float* target;        // training: target per rep
-  const __nv_bfloat16* params;
+  const bf16* params;
   float* out_f;               // inference: f per rep
   float* gpart;               // training: per-block gradient partials
   double* lpart;              // training: per-block loss partials
@@ -83,17 +92,44 @@ struct MlpArgs {
 };
 
 __device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+__device__ __forceinline__ uint32_t lds32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // lo in the low half (lower address)
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
+  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u));
+}
 
-// Stage the BF16 weights (pitch kWP) and the FP32 vectors in shared memory.
-__device__ void load_params(const __nv_bfloat16* __restrict__ p, unsigned char* sm) {
-  __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1);
-  __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(sm + kSmW2);
-  __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(sm + kSmW3);
+// D += A B on the tensor cores: A 16x16 (row), B 16x8 (col), BF16 in, FP32 accumulate.
+// Fragments (g = lane / 4, t = lane % 4): a = {A[g][2t..], A[g+8][2t..], A[g][2t+8..],
+// A[g+8][2t+8..]}, b = {B[2t..][g], B[2t+8..][g]}, d = {D[g][2t], D[g][2t+1], D[g+8][2t], D[g+8][2t+1]}.
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Four transposed 8x8 BF16 tiles: lane l gives the address of row (l % 8) of tile l / 8.
+__device__ __forceinline__ void ldsm4t(uint32_t (&r)[4], const bf16* p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(s));
+}
+
+// Stage the BF16 weights transposed (W^T[c][i]) and the FP32 vectors in shared memory.
+__device__ void load_params(const bf16* __restrict__ p, unsigned char* sm) {
+  bf16* w1 = reinterpret_cast<bf16*>(sm + kSmW1);
+  bf16* w2 = reinterpret_cast<bf16*>(sm + kSmW2);
+  bf16* w3 = reinterpret_cast<bf16*>(sm + kSmW3);
   float* vec = reinterpret_cast<float*>(sm + kSmVec);
-  for (int e = threadIdx.x; e < kIn * kHid; e += blockDim.x) w1[(e / kHid) * kWP + e % kHid] = p[kOffW1 + e];
+  for (int e = threadIdx.x; e < kIn * kHid; e += blockDim.x) w1[(e % kHid) * kXP + e / kHid] = p[kOffW1 + e];
   for (int e = threadIdx.x; e < kHid * kHid; e += blockDim.x) {
-    w2[(e / kHid) * kWP + e % kHid] = p[kOffW2 + e];
-    w3[(e / kHid) * kWP + e % kHid] = p[kOffW3 + e];
+    w2[(e % kHid) * kHP + e / kHid] = p[kOffW2 + e];
+    w3[(e % kHid) * kHP + e / kHid] = p[kOffW3 + e];
   }
   for (int e = threadIdx.x; e < kHid; e += blockDim.x) {
     vec[e] = __bfloat162float(p[kOffB1 + e]);
@@ -104,9 +140,9 @@ __device__ void load_params(const __nv_bfloat16* __restrict__ p, unsigned char* 
   if (threadIdx.x == 0) vec[4 * kHid] = __bfloat162float(p[kOffB4]);
 }
 
-// Inputs of the tile's 64 rows into xT[f][row]; rows past nrows get zeros.
-// Returns (through rep_of) nothing: the row -> rep map is r / SP.
-__device__ void tile_features(const MlpArgs& a, int64_t rep0, float* xT) {
+// Inputs of the tile's 64 rows into X[row][f] (BF16); rows past nreps get zeros.
+// Row r holds rotation r % SP of representative rep0 + r / SP.
+__device__ void tile_features(const MlpArgs& a, int64_t rep0, bf16* X) {
   const int r = threadIdx.x;
   if (r >= kTile) return;
   const int q = r / a.SP, s = r % a.SP;
@@ -136,109 +172,90 @@ __device__ void tile_features(const MlpArgs& a, int64_t rep0, float* xT) {
     x[3 * a.NOD + 1] = bf16r(sm.j2);
   }
 #pragma unroll
-  for (int f = 0; f < kIn; ++f) xT[f * kAP + r] = x[f];
+  for (int f = 0; f < kIn; f += 2)
+    *reinterpret_cast<uint32_t*>(X + r * kXP + f) = pack_bf16(x[f], x[f + 1]);
 }
 
-// outT[c][r] = tanh(b[c] + sum_k inT[k][r] W[k][c]) for the 64 x 128 tile.
-// Thread t: rows 4*(t/16) .. +3, columns 8*(t%16) .. +7.
-template <int K>
-__device__ __forceinline__ void layer_fwd(const float* __restrict__ inT, const __nv_bfloat16* __restrict__ W,
-                                          const float* __restrict__ bias, float* __restrict__ outT) {
-  const int rg = threadIdx.x >> 4, cg = threadIdx.x & 15;
-  const int r0 = 4 * rg, c0 = 8 * cg;
-  float acc[4][8];
+// OUT[r][c] = bf16(tanh(b[c] + sum_k IN[r][k] W[k][c])) for the 64 x 128 tile on
+// the tensor cores.  Warp w: rows 16 (w % 4) .. +15, columns 64 (w / 4) .. +63
+// (8 n-tiles); K = 16 (layer 1) or 128.  IN has pitch KP, W^T[c][k] too.
+template <int K, int KP>
+__device__ __forceinline__ void layer_fwd(const bf16* __restrict__ in, const bf16* __restrict__ Wt,
+                                          const float* __restrict__ bias, bf16* __restrict__ out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int rb = 16 * (warp & 3), cb = 64 * (warp >> 2);
+  float acc[8][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float b = bias[c0 + j];
+  for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) acc[i][j] = b;
-  }
-#pragma unroll 4
-  for (int k = 0; k < K; ++k) {
-    const float4 a = *reinterpret_cast<const float4*>(inT + k * kAP + r0);
-    const __nv_bfloat162* wr = reinterpret_cast<const __nv_bfloat162*>(W + k * kWP + c0);
-    float w[8];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const float2 f = __bfloat1622float2(wr[u]);
-      w[2 * u] = f.x;
-      w[2 * u + 1] = f.y;
-    }
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint32_t a[4];
+    a[0] = lds32(in + (rb + g) * KP + k0 + 2 * t);
+    a[1] = lds32(in + (rb + g + 8) * KP + k0 + 2 * t);
+    a[2] = lds32(in + (rb + g) * KP + k0 + 2 * t + 8);
+    a[3] = lds32(in + (rb + g + 8) * KP + k0 + 2 * t + 8);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      acc[0][j] = fmaf(a.x, w[j], acc[0][j]);
-      acc[1][j] = fmaf(a.y, w[j], acc[1][j]);
-      acc[2][j] = fmaf(a.z, w[j], acc[2][j]);
-      acc[3][j] = fmaf(a.w, w[j], acc[3][j]);
+      const bf16* wr = Wt + (cb + 8 * j + g) * KP + k0 + 2 * t;
+      mma_bf16(acc[j], a, lds32(wr), lds32(wr + 8));
     }
   }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    float4 o;
-    o.x = tanhf(acc[0][j]);
-    o.y = tanhf(acc[1][j]);
-    o.z = tanhf(acc[2][j]);
-    o.w = tanhf(acc[3][j]);
-    *reinterpret_cast<float4*>(outT + (c0 + j) * kAP + r0) = o;
+    const int c = cb + 8 * j + 2 * t;
+    const float b0 = bias[c], b1 = bias[c + 1];
+    *reinterpret_cast<uint32_t*>(out + (rb + g) * kHP + c) = pack_bf16(tanhf(acc[j][0] + b0), tanhf(acc[j][1] + b1));
+    *reinterpret_cast<uint32_t*>(out + (rb + g + 8) * kHP + c) =
+        pack_bf16(tanhf(acc[j][2] + b0), tanhf(acc[j][3] + b1));
   }
 }
 
-// out[r] = b4 + sum_c w4[c] h3[c][r]: 4 threads per row, shuffle reduction.
-__device__ __forceinline__ void layer_out(const float* __restrict__ h3T, const float* __restrict__ w4, float b4,
+// out[r] = b4 + sum_c w4[c] H3[r][c] (FP32): 4 threads per row, shuffle reduction.
+__device__ __forceinline__ void layer_out(const bf16* __restrict__ h3, const float* __restrict__ w4, float b4,
                                           float* __restrict__ out) {
   const int r = threadIdx.x >> 2, part = threadIdx.x & 3;
   float s = 0.f;
-#pragma unroll 8
-  for (int c = part; c < kHid; c += 4) s = fmaf(w4[c], h3T[c * kAP + r], s);
+#pragma unroll 4
+  for (int c = 2 * part; c < kHid; c += 8) {
+    const float2 h = unpack_bf16(lds32(h3 + r * kHP + c));
+    s = fmaf(w4[c], h.x, fmaf(w4[c + 1], h.y, s));
+  }
   s += __shfl_xor_sync(0xffffffffu, s, 1);
   s += __shfl_xor_sync(0xffffffffu, s, 2);
   if (part == 0) out[r] = s + b4;
 }
 
-__device__ __forceinline__ void forward_tile(const MlpArgs& a, unsigned char* sm, float* h3T, float* out) {
-  const __nv_bfloat16* w1 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW1);
-  const __nv_bfloat16* w2 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW2);
-  const __nv_bfloat16* w3 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW3);
+__device__ __forceinline__ void forward_tile(unsigned char* sm, bf16* h3, float* out) {
+  const bf16* w1 = reinterpret_cast<const bf16*>(sm + kSmW1);
+  const bf16* w2 = reinterpret_cast<const bf16*>(sm + kSmW2);
+  const bf16* w3 = reinterpret_cast<const bf16*>(sm + kSmW3);
   const float* vec = reinterpret_cast<const float*>(sm + kSmVec);
-  float* xT = reinterpret_cast<float*>(sm + kSmX);
-  float* h1T = reinterpret_cast<float*>(sm + kSmH1);
-  float* h2T = reinterpret_cast<float*>(sm + kSmH2);
-  layer_fwd<kIn>(xT, w1, vec, h1T);
+  const bf16* X = reinterpret_cast<const bf16*>(sm + kSmX);
+  bf16* h1 = reinterpret_cast<bf16*>(sm + kSmH1);
+  bf16* h2 = reinterpret_cast<bf16*>(sm + kSmH2);
+  layer_fwd<kIn, kXP>(X, w1, vec, h1);
   __syncthreads();
-  layer_fwd<kHid>(h1T, w2, vec + kHid, h2T);
+  layer_fwd<kHid, kHP>(h1, w2, vec + kHid, h2);
   __syncthreads();
-  layer_fwd<kHid>(h2T, w3, vec + 2 * kHid, h3T);
+  layer_fwd<kHid, kHP>(h2, w3, vec + 2 * kHid, h3);
   __syncthreads();
-  layer_out(h3T, vec + 3 * kHid, vec[4 * kHid], out);
+  layer_out(h3, vec + 3 * kHid, vec[4 * kHid], out);
   __syncthreads();
 }
 
 __global__ void __launch_bounds__(kThreads) k_mlp_forward(MlpArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   load_params(a.params, sm);
-  float* xT = reinterpret_cast<float*>(sm + kSmX);
-  float* h3T = reinterpret_cast<float*>(sm + kSmH1);  // inference reuses h1 for h3
-  float* out = reinterpret_cast<float*>(sm + kSmInfer);
+  bf16* X = reinterpret_cast<bf16*>(sm + kSmX);
+  bf16* h3 = reinterpret_cast<bf16*>(sm + kSmH1);  // inference reuses H1 for H3
+  float* out = reinterpret_cast<float*>(sm + kSmH3);
   const int per = kTile / a.SP;
   const int64_t ntiles = (a.nreps + per - 1) / per;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     __syncthreads();
-    tile_features(a, t * per, xT);
+    tile_features(a, t * per, X);
     __syncthreads();
-    const __nv_bfloat16* w1 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW1);
-    const __nv_bfloat16* w2 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW2);
-    const __nv_bfloat16* w3 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW3);
-    const float* vec = reinterpret_cast<const float*>(sm + kSmVec);
-    float* h1T = reinterpret_cast<float*>(sm + kSmH1);
-    float* h2T = reinterpret_cast<float*>(sm + kSmH2);
-    layer_fwd<kIn>(xT, w1, vec, h1T);
-    __syncthreads();
-    layer_fwd<kHid>(h1T, w2, vec + kHid, h2T);
-    __syncthreads();
-    layer_fwd<kHid>(h2T, w3, vec + 2 * kHid, h3T);
-    __syncthreads();
-    layer_out(h3T, vec + 3 * kHid, vec[4 * kHid], out);
-    __syncthreads();
+    forward_tile(sm, h3, out);
     if (threadIdx.x < per) {
       const int64_t b = t * per + threadIdx.x;
       if (b < a.nreps) {
@@ -250,94 +267,98 @@ __global__ void __launch_bounds__(kThreads) k_mlp_forward(MlpArgs a) {
   }
 }
 
-// dW[i][c] (+)= sum_r inT[i][r] gT[c][r] and db[c] (+)= sum_r gT[c][r] into
-// the block's partial.  Thread t: i = t/16 + 16u (u < K/16), c = t%16 + 16v.
-template <int K>
-__device__ __forceinline__ void grad_w(const float* __restrict__ inT, const float* __restrict__ gT,
+// dW[i][c] (+)= sum_r IN[r][i] DZ[r][c] on the tensor cores (M = KI inputs,
+// N = 128, K = 64 rows); both operands come transposed from their row-major
+// tiles through ldmatrix.trans.  KI = 128: warp w owns inputs 16 w .. +15 and
+// all 16 n-tiles; KI = 16: one m-tile, warp w owns columns 16 w .. +15.
+// db[c] (+)= sum_r DZ[r][c].  gW, gb: the block's FP32 partial (no other block
+// touches it).
+template <int KI, int KP>
+__device__ __forceinline__ void grad_w(const bf16* __restrict__ in, const bf16* __restrict__ dz,
                                        float* __restrict__ gW, float* __restrict__ gb) {
-  constexpr int NU = K / 16;
-  const int ig = threadIdx.x >> 4, cg = threadIdx.x & 15;
-  float acc[NU][8];
+  constexpr int NT = (KI == kHid) ? 16 : 2;  // n-tiles per warp
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int i0 = (KI == kHid) ? 16 * warp : 0;
+  const int c0w = (KI == kHid) ? 0 : 16 * warp;
+  float acc[NT][4];
 #pragma unroll
-  for (int u = 0; u < NU; ++u)
+  for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  const int lr = (lane & 7), lsel = (lane >> 3) & 1, lhi = lane >> 4;
 #pragma unroll
-    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
-  for (int r = 0; r < kTile; r += 4) {
-    float4 gv[8];
+  for (int r0 = 0; r0 < kTile; r0 += 16) {
+    uint32_t a[4];
+    ldsm4t(a, in + (r0 + lr + 8 * lhi) * KP + i0 + 8 * lsel);  // A[i][r] = IN[r][i]
 #pragma unroll
-    for (int v = 0; v < 8; ++v) gv[v] = *reinterpret_cast<const float4*>(gT + (cg + 16 * v) * kAP + r);
-#pragma unroll
-    for (int u = 0; u < NU; ++u) {
-      const float4 x = *reinterpret_cast<const float4*>(inT + (ig + 16 * u) * kAP + r);
-#pragma unroll
-      for (int v = 0; v < 8; ++v) {
-        float s = acc[u][v];
-        s = fmaf(x.x, gv[v].x, s);
-        s = fmaf(x.y, gv[v].y, s);
-        s = fmaf(x.z, gv[v].z, s);
-        s = fmaf(x.w, gv[v].w, s);
-        acc[u][v] = s;
-      }
+    for (int jj = 0; jj < NT / 2; ++jj) {
+      uint32_t b[4];
+      ldsm4t(b, dz + (r0 + lr + 8 * lsel) * kHP + c0w + 16 * jj + 8 * lhi);  // B[r][c] = DZ[r][c]
+      mma_bf16(acc[2 * jj], a, b[0], b[1]);
+      mma_bf16(acc[2 * jj + 1], a, b[2], b[3]);
     }
   }
 #pragma unroll
-  for (int u = 0; u < NU; ++u)
-#pragma unroll
-    for (int v = 0; v < 8; ++v) gW[(ig + 16 * u) * kHid + cg + 16 * v] += acc[u][v];
+  for (int j = 0; j < NT; ++j) {
+    const int c = c0w + 8 * j + 2 * t;
+    gW[(i0 + g) * kHid + c] += acc[j][0];
+    gW[(i0 + g) * kHid + c + 1] += acc[j][1];
+    gW[(i0 + g + 8) * kHid + c] += acc[j][2];
+    gW[(i0 + g + 8) * kHid + c + 1] += acc[j][3];
+  }
   if (threadIdx.x < kHid) {
     float s = 0.f;
-    for (int r = 0; r < kTile; ++r) s += gT[threadIdx.x * kAP + r];
+    for (int r = 0; r < kTile; ++r) s += __bfloat162float(dz[r * kHP + threadIdx.x]);
     gb[threadIdx.x] += s;
   }
 }
 
-// dz_prev[i][r] = (sum_c gT[c][r] W[i][c]) * (1 - h[i][r]^2), written over hT.
-// Thread t: rows 4*(t/16) .. +3, i = t%16 + 16u.
-__device__ __forceinline__ void back_data(const float* __restrict__ gT, const __nv_bfloat16* __restrict__ W,
-                                          float* hT) {
-  const int rg = threadIdx.x >> 4, ig = threadIdx.x & 15;
-  const int r0 = 4 * rg;
+// DZ_prev[r][i] = bf16((sum_c DZ[r][c] W[i][c]) * (1 - H[r][i]^2)), written over H
+// (each element is read and written by the thread that computes it).  M = 64,
+// N = 128 inputs, K = 128; warp w: rows 16 (w % 4) .., inputs 64 (w / 4) ..;
+// B[c][i] = W[i][c] = W^T[c][i] through ldmatrix.trans.
+__device__ __forceinline__ void back_data(const bf16* __restrict__ dz, const bf16* __restrict__ Wt, bf16* h) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int rb = 16 * (warp & 3), ib = 64 * (warp >> 2);
+  const int lr = (lane & 7), lsel = (lane >> 3) & 1, lhi = lane >> 4;
   float acc[8][4];
 #pragma unroll
-  for (int u = 0; u < 8; ++u)
-#pragma unroll
-    for (int i = 0; i < 4; ++i) acc[u][i] = 0.f;
+  for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
 #pragma unroll 2
-  for (int c = 0; c < kHid; ++c) {
-    const float4 g = *reinterpret_cast<const float4*>(gT + c * kAP + r0);
+  for (int c0 = 0; c0 < kHid; c0 += 16) {
+    uint32_t a[4];
+    a[0] = lds32(dz + (rb + g) * kHP + c0 + 2 * t);
+    a[1] = lds32(dz + (rb + g + 8) * kHP + c0 + 2 * t);
+    a[2] = lds32(dz + (rb + g) * kHP + c0 + 2 * t + 8);
+    a[3] = lds32(dz + (rb + g + 8) * kHP + c0 + 2 * t + 8);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const float w = __bfloat162float(W[(ig + 16 * u) * kWP + c]);
-      acc[u][0] = fmaf(g.x, w, acc[u][0]);
-      acc[u][1] = fmaf(g.y, w, acc[u][1]);
-      acc[u][2] = fmaf(g.z, w, acc[u][2]);
-      acc[u][3] = fmaf(g.w, w, acc[u][3]);
+    for (int jj = 0; jj < 4; ++jj) {
+      uint32_t b[4];
+      ldsm4t(b, Wt + (c0 + lr + 8 * lsel) * kHP + ib + 16 * jj + 8 * lhi);
+      mma_bf16(acc[2 * jj], a, b[0], b[1]);
+      mma_bf16(acc[2 * jj + 1], a, b[2], b[3]);
     }
   }
-  __syncthreads();  // every thread has read gT; hT is overwritten below (hT != gT)
 #pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    float4* hp = reinterpret_cast<float4*>(hT + (ig + 16 * u) * kAP + r0);
-    float4 h = *hp;
-    h.x = acc[u][0] * (1.f - h.x * h.x);
-    h.y = acc[u][1] * (1.f - h.y * h.y);
-    h.z = acc[u][2] * (1.f - h.z * h.z);
-    h.w = acc[u][3] * (1.f - h.w * h.w);
-    *hp = h;
+  for (int j = 0; j < 8; ++j) {
+    const int i = ib + 8 * j + 2 * t;
+    uint32_t* p0 = reinterpret_cast<uint32_t*>(h + (rb + g) * kHP + i);
+    uint32_t* p1 = reinterpret_cast<uint32_t*>(h + (rb + g + 8) * kHP + i);
+    const float2 h0 = unpack_bf16(*p0), h1 = unpack_bf16(*p1);
+    *p0 = pack_bf16(acc[j][0] * (1.f - h0.x * h0.x), acc[j][1] * (1.f - h0.y * h0.y));
+    *p1 = pack_bf16(acc[j][2] * (1.f - h1.x * h1.x), acc[j][3] * (1.f - h1.y * h1.y));
   }
 }
 
 __global__ void __launch_bounds__(kThreads) k_mlp_train(MlpArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   load_params(a.params, sm);
-  const __nv_bfloat16* w2 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW2);
-  const __nv_bfloat16* w3 = reinterpret_cast<const __nv_bfloat16*>(sm + kSmW3);
+  const bf16* w2 = reinterpret_cast<const bf16*>(sm + kSmW2);
+  const bf16* w3 = reinterpret_cast<const bf16*>(sm + kSmW3);
   const float* vec = reinterpret_cast<const float*>(sm + kSmVec);
-  float* xT = reinterpret_cast<float*>(sm + kSmX);
-  float* h1T = reinterpret_cast<float*>(sm + kSmH1);
-  float* h2T = reinterpret_cast<float*>(sm + kSmH2);
-  float* h3T = reinterpret_cast<float*>(sm + kSmH3);
-  float* gT = reinterpret_cast<float*>(sm + kSmG);
+  bf16* X = reinterpret_cast<bf16*>(sm + kSmX);
+  bf16* h1 = reinterpret_cast<bf16*>(sm + kSmH1);
+  bf16* h2 = reinterpret_cast<bf16*>(sm + kSmH2);
+  bf16* h3 = reinterpret_cast<bf16*>(sm + kSmH3);
+  bf16* G = reinterpret_cast<bf16*>(sm + kSmG);
   float* out = reinterpret_cast<float*>(sm + kSmRow);
   float* dout = out + kTile;
   float* gp = a.gpart + (size_t)blockIdx.x * kNP;
@@ -346,9 +367,9 @@ __global__ void __launch_bounds__(kThreads) k_mlp_train(MlpArgs a) {
   double loss = 0.0;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     __syncthreads();
-    tile_features(a, t * per, xT);
+    tile_features(a, t * per, X);
     __syncthreads();
-    forward_tile(a, sm, h3T, out);
+    forward_tile(sm, h3, out);
     // per representative: f = mean over rotations; loss and dL/dout
     if (threadIdx.x < kTile) {
       const int r = threadIdx.x, q = r / a.SP, s = r % a.SP;
@@ -366,17 +387,17 @@ __global__ void __launch_bounds__(kThreads) k_mlp_train(MlpArgs a) {
       dout[r] = d;
     }
     __syncthreads();
-    // output layer: dw4, db4; dz3 = dout * w4 * (1 - h3^2) into gT
+    // output layer: dw4, db4; dz3 = bf16(dout * w4 * (1 - h3^2)) into G
     if (threadIdx.x < kHid) {
       const int c = threadIdx.x;
-      float s = 0.f;
-      for (int r = 0; r < kTile; ++r) s = fmaf(dout[r], h3T[c * kAP + r], s);
-      gp[kOffW4 + c] += s;
       const float w4 = vec[3 * kHid + c];
+      float s = 0.f;
       for (int r = 0; r < kTile; ++r) {
-        const float h = h3T[c * kAP + r];
-        gT[c * kAP + r] = dout[r] * w4 * (1.f - h * h);
+        const float h = __bfloat162float(h3[r * kHP + c]);
+        s = fmaf(dout[r], h, s);
+        G[r * kHP + c] = __float2bfloat16_rn(dout[r] * w4 * (1.f - h * h));
       }
+      gp[kOffW4 + c] += s;
     }
     if (threadIdx.x == kHid) {
       float s = 0.f;
@@ -384,36 +405,15 @@ __global__ void __launch_bounds__(kThreads) k_mlp_train(MlpArgs a) {
       gp[kOffB4] += s;
     }
     __syncthreads();
-    grad_w<kHid>(h2T, gT, gp + kOffW3, gp + kOffB3);
+    grad_w<kHid, kHP>(h2, G, gp + kOffW3, gp + kOffB3);
     __syncthreads();
-    back_data(gT, w3, h2T);   // h2T <- dz2
+    back_data(G, w3, h2);   // h2 <- dz2
     __syncthreads();
-    grad_w<kHid>(h1T, h2T, gp + kOffW2, gp + kOffB2);
+    grad_w<kHid, kHP>(h1, h2, gp + kOffW2, gp + kOffB2);
     __syncthreads();
-    back_data(h2T, w2, h1T);  // h1T <- dz1
+    back_data(h2, w2, h1);  // h1 <- dz1
     __syncthreads();
-    // dW1 (16 x 128): i = t/16, c = t%16 + 16v
-    {
-      const int i = threadIdx.x >> 4, cg = threadIdx.x & 15;
-      float acc[8];
-#pragma unroll
-      for (int v = 0; v < 8; ++v) acc[v] = 0.f;
-      for (int r = 0; r < kTile; r += 4) {
-        const float4 x = *reinterpret_cast<const float4*>(xT + i * kAP + r);
-#pragma unroll
-        for (int v = 0; v < 8; ++v) {
-          const float4 g = *reinterpret_cast<const float4*>(h1T + (cg + 16 * v) * kAP + r);
-          acc[v] = fmaf(x.x, g.x, fmaf(x.y, g.y, fmaf(x.z, g.z, fmaf(x.w, g.w, acc[v]))));
-        }
-      }
-#pragma unroll
-      for (int v = 0; v < 8; ++v) gp[kOffW1 + i * kHid + cg + 16 * v] += acc[v];
-      if (threadIdx.x < kHid) {
-        float s = 0.f;
-        for (int r = 0; r < kTile; ++r) s += h1T[threadIdx.x * kAP + r];
-        gp[kOffB1 + threadIdx.x] += s;
-      }
-    }
+    grad_w<kIn, kXP>(X, h1, gp + kOffW1, gp + kOffB1);
   }
   __shared__ double lsh[kThreads];
   lsh[threadIdx.x] = loss;
@@ -745,7 +745,7 @@ void Mlp::forward(const uint64_t* d_c, const int* d_s, const MlpSample* d_smp, c
   static bool attr = false;
   if (!attr) {
     QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(kSmInfer + 2 * kTile * 4)));
+                                         (int)kSmInfer));
     attr = true;
   }
   MlpArgs a{};
@@ -754,7 +754,7 @@ void Mlp::forward(const uint64_t* d_c, const int* d_s, const MlpSample* d_smp, c
   const int per = kTile / a.SP;
   const int64_t ntiles = (n + per - 1) / per;
   const int nblk = (int)std::min<int64_t>((int64_t)sm_count() * 8, ntiles);
-  k_mlp_forward<<<nblk, kThreads, kSmInfer + 2 * kTile * 4, st>>>(a);
+  k_mlp_forward<<<nblk, kThreads, kSmInfer, st>>>(a);
   check_launch("k_mlp_forward");
 }
 

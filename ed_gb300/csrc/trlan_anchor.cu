@@ -41,7 +41,8 @@ namespace qs3g {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kChunks = 304;  // row chunks of the overlap kernels (2 per SM)
+constexpr int kChunks = 304;       // row chunks of the overlap kernels (2 per SM) ...
+constexpr int kChunksNarrow = 1216;  // ... and for one or two columns (8 per SM, to fill the GPU)
 
 __device__ __forceinline__ float4 split2(double2 v) {
   const float2 r = dsplit(v.x), i = dsplit(v.y);
@@ -316,7 +317,7 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   sc.ensure(NOM + 2);
   Ops<double2> o64{st, sc.part.get(), true, real};
   Ops<float2> o32{st, sc.part.get(), false, real};
-  DevBuf<double2> part((size_t)kChunks * 4 * (NOM + 2));
+  DevBuf<double2> part(std::max<size_t>((size_t)kChunks * 2 * (NOM + 2), (size_t)kChunksNarrow * 4));
   // device scalars
   const int NS = NOM + 2;
   DevBuf<double2> dsc((size_t)NS * (NOM + 12));  // the regions below, in this order
@@ -336,7 +337,7 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   // conj(W[:, c0 .. c0+ncols)) . (v0, v1) into out[v * ncols + c]
   auto ovl = [&](int c0, int ncols, const double2* v0, const double2* v1, double2* outp) {
     const int64_t tiles = (n + kT - 1) / kT;
-    const int nb = (int)std::min<int64_t>(kChunks, tiles);
+    const int nb = (int)std::min<int64_t>(ncols <= 2 ? kChunksNarrow : kChunks, tiles);
     const int64_t rows = (tiles + nb - 1) / nb * kT;
     const dim3 grid((unsigned)((ncols + 1) / 2), (unsigned)nb);
     if (real) k_anchor_ovl<true><<<grid, kT, 0, st>>>(col(c0), ldv, ncols, v0, v1, n, rows, part.get());

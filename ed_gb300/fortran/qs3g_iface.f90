@@ -70,6 +70,15 @@ module qs3g_iface
       real(c_double) :: list_r(*)
     end function
 
+    ! real FP32 product (H - shift) v1 for k = 0 chain / U(1) sectors
+    integer(c_int) function qs3g_hv32_real(h, v0, v1, shift, where) bind(C, name="qs3g_hv32_real")
+      import :: c_ptr, c_int, c_float
+      type(c_ptr), value :: h
+      real(c_float) :: v0(*), v1(*)
+      real(c_float) :: shift
+      integer(c_int) :: where
+    end function
+
     ! wall-clock limit of qs3g_trlan, and what the last qs3g_trlan did
     integer(c_int) function qs3g_set_time_limit(h, seconds) bind(C, name="qs3g_set_time_limit")
       import :: c_ptr, c_int, c_double

@@ -140,6 +140,13 @@ int qs3g_hv32(qs3g_handle h, qs3g_cplx32* v0, const qs3g_cplx32* v1, const int* 
  * vectors are complex(8) for every sector. */
 int qs3g_hv_real(qs3g_handle h, double* v0, const double* v1, const int* where);
 
+/* The real product in FP32 (D floats): v0 = (H - shift) v1 with the shift
+ * subtracted from the diagonal in FP64 before it is rounded (shift may be
+ * NULL: 0), for sectors whose H is real symmetric (QS3G_ENOTSUP otherwise).
+ * The Krylov vectors of qs3g_trlan precision 1 + QS3G_REAL go through this
+ * product.  No counterpart in the reference, whose vectors are complex(8). */
+int qs3g_hv32_real(qs3g_handle h, float* v0, const float* v1, const float* shift, const int* where);
+
 /* Schedule of the H*v kernel for the current general-lattice sector (chains
  * and U(1) sectors use one thread per row always): 0 = autotune (the first
  * product of each precision times a warp per row, lanes over the

@@ -3,7 +3,10 @@ start-vector network (ed_gb300/csrc/mlp.cu), used to check the GPU's forward
 pass, loss and gradients.  Only tests/ may import it.
 
 It follows the same definitions: inputs and parameters rounded to BF16
-(round to nearest even), hidden activations tanh, output = mean over the NOD
+(round to nearest even), hidden activations tanh rounded to BF16 (the GPU
+keeps them as BF16 tensor-core operands), back-propagated signals
+dz = dL/d(pre-activation) rounded to BF16 before they enter a matrix
+product, output = mean over the NOD
 cyclic rotations of the gap sequence, loss = mean over representatives of
 (f - t)^2, targets t = Re(psi * phase) * list_r / L * sqrt(C(L, NOD)) with the
 phase that makes the largest-modulus amplitude real and the sign that makes
@@ -74,11 +77,14 @@ def features(confs, L, delta, j2, q0):
     return X.reshape(n * nod, IN)
 
 
-def forward(p, X, nod, round_params=True):
+def forward(p, X, nod, round_params=True, round_acts=True):
+    """round_acts=False: exact float64 activations (the smooth function whose
+    gradient the finite-difference test checks); True: BF16 as on the GPU."""
+    rd = bf16 if round_acts else (lambda v: v)
     W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p, round_params)
-    h1 = np.tanh(X @ W1 + b1)
-    h2 = np.tanh(h1 @ W2 + b2)
-    h3 = np.tanh(h2 @ W3 + b3)
+    h1 = rd(np.tanh(X @ W1 + b1))
+    h2 = rd(np.tanh(h1 @ W2 + b2))
+    h3 = rd(np.tanh(h2 @ W3 + b3))
     out = h3 @ w4 + b4
     f = out.reshape(-1, nod).mean(axis=1)
     return f, (h1, h2, h3)
@@ -99,10 +105,14 @@ def targets(psi, list_r, confs, L, nod, q0):
     return (re * np.asarray(list_r) * scale).astype(np.float32).astype(np.float64)
 
 
-def loss_grad(p, X, t, nod, round_params=True):
-    """Mean squared error over representatives and its gradient (NPARAMS)."""
+def loss_grad(p, X, t, nod, round_params=True, round_acts=True):
+    """Mean squared error over representatives and its gradient (NPARAMS).
+    With round_acts the activations and the back-propagated signals are
+    rounded to BF16 where the GPU rounds them (the gradient of the rounded
+    forward pass taken through the roundings)."""
+    rd = bf16 if round_acts else (lambda v: v)
     W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p, round_params)
-    f, (h1, h2, h3) = forward(p, X, nod, round_params)
+    f, (h1, h2, h3) = forward(p, X, nod, round_params, round_acts)
     B = len(t)
     e = f - t
     loss = float(np.sum(e * e) / B)
@@ -110,13 +120,13 @@ def loss_grad(p, X, t, nod, round_params=True):
     g = np.zeros(NPARAMS)
     g[OFF_W4:OFF_B4] = h3.T @ dout
     g[OFF_B4] = dout.sum()
-    dz3 = np.outer(dout, w4) * (1 - h3 * h3)
+    dz3 = rd(np.outer(dout, w4) * (1 - h3 * h3))
     g[OFF_W3:OFF_B3] = (h2.T @ dz3).reshape(-1)
     g[OFF_B3:OFF_W4] = dz3.sum(axis=0)
-    dz2 = (dz3 @ W3.T) * (1 - h2 * h2)
+    dz2 = rd((dz3 @ W3.T) * (1 - h2 * h2))
     g[OFF_W2:OFF_B2] = (h1.T @ dz2).reshape(-1)
     g[OFF_B2:OFF_W3] = dz2.sum(axis=0)
-    dz1 = (dz2 @ W2.T) * (1 - h1 * h1)
+    dz1 = rd((dz2 @ W2.T) * (1 - h1 * h1))
     g[OFF_W1:OFF_B1] = (X.T @ dz1).reshape(-1)
     g[OFF_B1:OFF_W2] = dz1.sum(axis=0)
     return loss, g

@@ -81,3 +81,22 @@ def test_anchored_from_a_start_vector(qs3g):
     assert abs(rr["ene"][0] - rs["ene"][0]) <= 1e-10 * abs(rr["ene"][0])
     assert rs["iters"] < rr["iters"]
     h.close()
+
+
+def test_hv32_real_matches_oracle(qs3g):
+    """qs3g_hv32_real: (H - shift) x in FP32 for real x, shift applied in FP64."""
+    from ed_gb300 import capi
+    L, nod = 20, 4
+    b, jxy, jz = inputs.chain_bonds(L, (1.0, 0.5), (0.3, 0.3))
+    om = O.Model(L, L, 1, 1, b, jxy, jz, kmax=nod + 2)
+    osec = om.build_sector(nod, (0, 0, 0))
+    h = capi.Handle(L, L, 1, 1, b, jxy, jz)
+    D = h.build_sector(nod, (0, 0, 0))
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(D).astype(np.float32)
+    sigma = 0.25 * jz.sum()
+    y0 = osec.hv(x.astype(np.complex128)).real - sigma * x.astype(np.float64)
+    y = h.hv32_real(x, shift=sigma)
+    assert np.abs(y - y0).max() <= 2e-6 * np.abs(y0).max()
+    assert np.abs(h.hv32_real(x) - osec.hv(x.astype(np.complex128)).real).max() <= 2e-6 * np.abs(y0).max() * 10
+    h.close()

@@ -2,9 +2,13 @@
 gradient against the float64 oracle (oracle/mlp_oracle.py), then training on
 small-L ground states and the gain of the predicted start vector.
 
-Tolerances: the GPU accumulates in float32 and the oracle in float64 on the
-same BF16-rounded inputs and parameters, so the loss agrees to 1e-5 relative
-and the gradient to 1e-4 in relative 2-norm.
+Tolerances: the GPU accumulates in float32 (tensor-core BF16 products) and
+the oracle in float64, with the same BF16 roundings of inputs, parameters,
+activations and back-propagated signals.  A value within an FP32 rounding of
+a BF16 tie can round to different neighbours on the two sides (one BF16 unit,
+2^-8 relative), so the loss agrees to 1e-4 relative and the gradient to
+2e-3 in relative 2-norm, per layer; a wrong fragment layout or a missing term
+would show as O(1).
 """
 import numpy as np
 import pytest
@@ -53,11 +57,11 @@ def test_mlp_loss_and_gradient_match_oracle(qs3g):
     X, t = np.concatenate(Xs), np.concatenate(ts)
     loss0, g0 = M.loss_grad(p, X, t, nod)
     loss1, g1 = net.loss_grad()
-    assert abs(loss1 - loss0) <= 1e-5 * loss0
-    assert np.linalg.norm(g1 - g0) <= 1e-4 * np.linalg.norm(g0)
+    assert abs(loss1 - loss0) <= 1e-4 * loss0
+    assert np.linalg.norm(g1 - g0) <= 2e-3 * np.linalg.norm(g0)
     # per-layer check so that no block of the gradient hides behind another's norm
     for a, b in [(M.OFF_W1, M.OFF_B1), (M.OFF_W2, M.OFF_B2), (M.OFF_W3, M.OFF_B3), (M.OFF_W4, M.OFF_B4 + 1)]:
-        assert np.linalg.norm(g1[a:b] - g0[a:b]) <= 1e-4 * np.linalg.norm(g0[a:b]) + 1e-12
+        assert np.linalg.norm(g1[a:b] - g0[a:b]) <= 2e-3 * np.linalg.norm(g0[a:b]) + 1e-12
     net.close()
 
 

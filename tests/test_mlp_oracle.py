@@ -32,7 +32,7 @@ def test_gradient_matches_finite_differences():
     X = M.features(confs, L, 0.7, 0.25, np.pi)
     t = rng.standard_normal(len(confs))
     p = M.init_params(rng)
-    loss, g = M.loss_grad(p, X, t, nod, round_params=False)
+    loss, g = M.loss_grad(p, X, t, nod, round_params=False, round_acts=False)
     idx = np.concatenate([rng.choice(np.arange(M.OFF_B1), 6, replace=False),
                           rng.choice(np.arange(M.OFF_W2, M.OFF_B2), 6, replace=False),
                           rng.choice(np.arange(M.OFF_W3, M.OFF_B3), 6, replace=False),
@@ -42,8 +42,8 @@ def test_gradient_matches_finite_differences():
         pp, pm = p.copy(), p.copy()
         pp[k] += eps
         pm[k] -= eps
-        lp, _ = M.loss_grad(pp, X, t, nod, round_params=False)
-        lm, _ = M.loss_grad(pm, X, t, nod, round_params=False)
+        lp, _ = M.loss_grad(pp, X, t, nod, round_params=False, round_acts=False)
+        lm, _ = M.loss_grad(pm, X, t, nod, round_params=False, round_acts=False)
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), (k, fd, g[k])
 
@@ -57,3 +57,17 @@ def test_output_is_translation_invariant():
     f0, _ = M.forward(p, M.features(c, L, 1.0, 0.2, np.pi), nod)
     f1, _ = M.forward(p, M.features(shifted, L, 1.0, 0.2, np.pi), nod)
     assert abs(f0[0] - f1[0]) < 1e-12
+
+
+def test_rounded_gradient_is_close_to_the_exact_one():
+    """The BF16 roundings of the activations and signals move the gradient by
+    about the BF16 unit (2^-8) relative, not more."""
+    rng = np.random.default_rng(2)
+    L, nod = 24, 4
+    confs = _confs(L, nod, 60, rng)
+    X = M.features(confs, L, 0.7, 0.25, np.pi)
+    t = rng.standard_normal(len(confs))
+    p = M.init_params(rng)
+    _, g0 = M.loss_grad(p, X, t, nod, round_acts=False)
+    _, g1 = M.loss_grad(p, X, t, nod, round_acts=True)
+    assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
