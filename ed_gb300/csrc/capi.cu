@@ -54,6 +54,45 @@ int guarded(qs3g_ctx* h, F&& f) {
   }
 }
 
+// A chain whose bonds are, for one or two distances o < NOS/2, exactly the
+// NOS bonds (s, s + o mod NOS) with one (Jxy, Jz) per distance: the H*v then
+// runs its hops as moves by +-o (hv.cu, k_hv_uchain*).
+void detect_uniform_chain(Model& m) {
+  m.uni_no = 0;
+  const int L = m.NOS;
+  if (!m.chain || L < 5 || m.NOxxz == 0) return;
+  std::vector<int> dist_of(m.NOxxz);
+  std::vector<int> offs;
+  for (int b = 0; b < m.NOxxz; ++b) {
+    const int o = m.p2[b] - m.p1[b];
+    const int dk = std::min(o, L - o);
+    if (dk <= 0 || 2 * dk >= L) return;  // self or half-ring bonds: general kernels
+    dist_of[b] = dk;
+    if (std::find(offs.begin(), offs.end(), dk) == offs.end()) offs.push_back(dk);
+  }
+  if (offs.size() > 2) return;
+  std::sort(offs.begin(), offs.end());
+  for (size_t k = 0; k < offs.size(); ++k) {
+    const int dk = offs[k];
+    std::vector<int> seen(L + 1, 0);
+    int first = -1;
+    for (int b = 0; b < m.NOxxz; ++b) {
+      if (dist_of[b] != dk) continue;
+      if (first < 0) first = b;
+      if (m.sJxy[b] != m.sJxy[first] || m.sJz[b] != m.sJz[first]) return;
+      // the site s with (s, s + dk mod L) = this bond
+      const int a = m.p1[b], c = m.p2[b];
+      const int s0 = (c - a == dk) ? a : c;
+      if (seen[s0]++) return;
+    }
+    for (int s0 = 1; s0 <= L; ++s0)
+      if (seen[s0] != 1) return;
+    m.uni_off[k] = dk;
+    m.uni_bond[k] = first;
+  }
+  m.uni_no = (int)offs.size();
+}
+
 // Site adjacency, per-site Jz sums and device copies of the bond data.
 void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int* p_xxz, const double* sJint,
                  cudaStream_t st) {
@@ -97,6 +136,7 @@ void setup_model(Model& m, int NOS, int LX, int LY, int LZ, int NOxxz, const int
   }
   m.Sz_all += comp_all;
   for (int i = 0; i <= NOS; ++i) m.Sz_site[i] += comp_site[i];
+  detect_uniform_chain(m);
   m.adj_off.assign(NOS + 2, 0);
   m.adj.clear();
   for (int s = 1; s <= NOS; ++s) {

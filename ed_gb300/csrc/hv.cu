@@ -62,6 +62,9 @@ struct HvArgs {
   const float* coefR32;    //         [b * (NOD + 1) + c]
   const double* invR;      // chains: 1 / list_r by self-translation count
   const float* invR32;
+  int uno;                 // uniform chains: number of bond distances (0: not uniform)
+  int uoff[2];             //   the distances
+  int ubond[2];            //   one bond of each distance (their couplings are equal)
 };
 
 constexpr int kHvThreads = 256;
@@ -178,7 +181,6 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
   const int L = a.L, half = a.L >> 1;
   R ax = 0, ay = 0;
-  uint64_t deferred = 0;  // bit 8 m + s: bond s (< 8) of spin m takes the general path
 #pragma unroll
   for (int m = 0; m < NOD; ++m) {
     const int d = n[m];
@@ -252,15 +254,6 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
           ell = (site == 1) ? 0 : L - site + 1;
         }
       } else {
-        // onto / past another spin, or a tie: the general path, after the loop
-        // (the lanes of a warp that need it then share one pass instead of
-        // stalling the others at every hop); bonds past the 8th of a site
-        // take it inline
-        const int slot = t - e0;
-        if (slot < 8) {
-          deferred |= 1ull << (8 * m + slot);
-          continue;
-        }
         bool edown = false;
 #pragma unroll
         for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
@@ -273,28 +266,181 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
       hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
     }
   }
-  while (deferred) {
-    const int b = __ffsll((long long)deferred) - 1;
-    deferred &= deferred - 1;
-    const int m = b >> 3;
-    int d = n[0];
+  const R ir = __ldg(invR + chain_self_count<NOD>(n, a.L, a.bits));
+  y[i] = row_out(di, xi, ir, ax, ay);
+}
+
+// Uniform chains: every site s carries a bond to s + o (mod L) for each of NO
+// distances o < L/2, with one coupling per distance (the chains of the XXZ
+// configs).  The hops of spin m are then the moves by +o and -o: no
+// adjacency list, no displacement arithmetic, and all NOD * NO * 2 hops are
+// unrolled, so their directory and x(id) loads are independent and can be
+// in flight together.  Hops that reach another spin or meet a tied largest
+// gap take the general path.  The sum runs over the same hops as
+// hv_chain_row, in another order.
+template <int NOD, int NO, bool KZERO, class V>
+__device__ __forceinline__ void hv_uchain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
+                                              const double* __restrict__ diag,
+                                              const typename Cplx<V>::R* __restrict__ coefR,
+                                              const typename Cplx<V>::R* __restrict__ invR,
+                                              const typename Cplx<V>::P* __restrict__ ph, int64_t i, double shift) {
+  using R = typename Cplx<V>::R;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  int g[NOD];
 #pragma unroll
-    for (int k = 1; k < NOD; ++k) d = (m == k) ? n[k] : d;
-    const uint32_t w = __ldg(a.adj + __ldg(a.adj_off + d) + (b & 7));
-    const int e = (int)(w & 0xffffu);
-    bool edown = false;
+  for (int k = 0; k < NOD - 1; ++k) g[k] = n[k + 1] - n[k];
+  g[NOD - 1] = n[0] + a.L - n[NOD - 1];
+  const V xi = x[i];
+  const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
+  const int L = a.L;
+  int off[NO];
+  R cf[NO];
 #pragma unroll
-    for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
-    if (edown) continue;  // parallel bond: diagonal only
-    int ell = 0, cnt = 1;
-    const int id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
-    if (id < 0) continue;
-    V xv = x[id];
-    if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
-    hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
+  for (int k = 0; k < NO; ++k) {
+    off[k] = a.uoff[k];
+    cf[k] = __ldg(coefR + a.ubond[k] * (NOD + 1) + 1);
+  }
+  R ax = 0, ay = 0;
+#pragma unroll
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    const int mp = (m + NOD - 1) % NOD;
+    const int gn = g[m], gp = g[mp];
+    int omax = -1, oarg = 0, oties = 0;
+#pragma unroll
+    for (int k = 0; k < NOD; ++k) {
+      if (k == m || k == mp) continue;
+      oties = (g[k] == omax) ? oties + 1 : ((g[k] > omax) ? 1 : oties);
+      oarg = (g[k] > omax) ? k : oarg;
+      omax = max(omax, g[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NO; ++k) {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir) {
+        const int o = off[k];
+        const int del = dir ? -o : o;
+        const int lm = gp + del, ln = gn - del;
+        const int mx = max(max(lm, ln), omax);
+        const int nmx = (lm == mx) + (ln == mx) + (omax == mx ? oties : 0);
+        int id, ell = 0, cnt = 1;
+        R cc = cf[k];
+        if ((dir ? o < gp : o < gn) && nmx == 1) {
+          uint32_t idx = 0;
+          const bool cA = (lm == mx), cB = (ln == mx);
+          if constexpr (NOD == 4) {
+            const int m1 = (m + 1) % NOD, m2 = (m + 2) % NOD;
+            const bool o1 = (oarg == m1);
+            const int G1 = cA ? ln : (cB ? g[m1] : (o1 ? g[m2] : lm));
+            const int G12 = cA ? ln + g[m1] : (cB ? g[m1] + g[m2] : (o1 ? g[m2] + lm : lm + ln));
+            const uint32_t x2 = (uint32_t)(G12 - 1);
+            idx = (uint32_t)(G1 - 1) + ((x2 * (x2 - 1u)) >> 1) +
+                  __ldg(a.binomA + 2 * (size_t)(L - 1) + (L - 1 - mx));
+          } else {
+            const int c = cA ? mp : (cB ? m : oarg);
+            int pj = 1;
+#pragma unroll
+            for (int j = 1; j < NOD; ++j) {
+              int lane = 0;
+              if (j == NOD - 1) {
+                lane = L - mx - (pj - 1);
+              } else {
+#pragma unroll
+                for (int q = 0; q < NOD; ++q) {
+                  const int vq = (q == mp) ? lm : ((q == m) ? ln : g[q]);
+                  lane = (c == (q - j + NOD) % NOD) ? vq : lane;
+                }
+              }
+              pj += lane;
+              const uint32_t xj = (uint32_t)(pj - 2);
+              if (j == 1) idx += xj;
+              else if (j == 2) idx += (xj * (xj - 1u)) >> 1;
+              else idx += __ldg(a.binomA + (size_t)(j - 1) * (L - 1) + xj);
+            }
+          }
+          id = dir_lookup32(a.dir, idx);
+          if constexpr (!KZERO) {
+            const int c = cA ? mp : (cB ? m : oarg);
+            const int sw = (c + 1) % NOD;  // the spin that goes to site 1
+            int e = d + del;
+            e = (e > L) ? e - L : ((e < 1) ? e + L : e);
+            int site = n[0];
+#pragma unroll
+            for (int q = 1; q < NOD; ++q) site = (sw == q) ? n[q] : site;
+            site = (sw == m) ? e : site;
+            ell = (site == 1) ? 0 : L - site + 1;
+          }
+        } else {
+          int e = d + del;
+          e = (e > L) ? e - L : ((e < 1) ? e + L : e);
+          bool edown = false;
+#pragma unroll
+          for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+          if (edown) continue;  // parallel bond: diagonal only
+          id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+          cc = __ldg(coefR + a.ubond[k] * (NOD + 1) + cnt);
+        }
+        if (id < 0) continue;
+        V xv = x[id];
+        if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+        hop_acc(cc, xv, ax, ay);
+      }
+    }
   }
   const R ir = __ldg(invR + chain_self_count<NOD>(n, a.L, a.bits));
   y[i] = row_out(di, xi, ir, ax, ay);
+}
+
+template <int NOD, int NO, bool KZERO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_uchain64(HvArgs a, const double2* __restrict__ x,
+                                                            double2* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  hv_uchain_row<NOD, NO, KZERO, double2>(a, x, y, a.diag, a.coefR, a.invR, a.chainph, i, 0.0);
+}
+
+template <int NOD, int NO, bool KZERO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_uchain32(HvArgs a, const float2* __restrict__ x,
+                                                            float2* __restrict__ y, float shift) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  hv_uchain_row<NOD, NO, KZERO, float2>(a, x, y, a.diag, a.coefR32, a.invR32, a.chainph32, i, (double)shift);
+}
+
+template <int NOD, int NO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_uchain64r(HvArgs a, const double* __restrict__ x,
+                                                             double* __restrict__ y, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_uchain_row<NOD, NO, true, double>(a, x, y, a.diag, a.coefR, a.invR, nullptr, i, 0.0);
+  else if (i == a.D && pad) y[i] = 0.0;
+}
+
+template <int NOD, int NO>
+__global__ void __launch_bounds__(kHvThreads) k_hv_uchain32r(HvArgs a, const float* __restrict__ x,
+                                                             float* __restrict__ y, float shift, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.D) hv_uchain_row<NOD, NO, true, float>(a, x, y, a.diag, a.coefR32, a.invR32, nullptr, i, (double)shift);
+  else if (i == a.D && pad) y[i] = 0.f;
+}
+
+// f(NOD, NO) for a uniform chain sector with 2 <= NOD <= 6 and 1 <= NO <= 2;
+// false when the sector takes the general chain kernels.
+template <class F>
+bool dispatch_uniform(const Model& m, const Sector& s, F&& f) {
+  if (!s.anchored || m.uni_no < 1 || m.uni_no > 2 || s.NOD < 2 || s.NOD > 6) return false;
+  auto with_no = [&](auto nod) {
+    if (m.uni_no == 1) f(nod, std::integral_constant<int, 1>{});
+    else f(nod, std::integral_constant<int, 2>{});
+  };
+  switch (s.NOD) {
+    case 2: with_no(std::integral_constant<int, 2>{}); break;
+    case 3: with_no(std::integral_constant<int, 3>{}); break;
+    case 4: with_no(std::integral_constant<int, 4>{}); break;
+    case 5: with_no(std::integral_constant<int, 5>{}); break;
+    default: with_no(std::integral_constant<int, 6>{}); break;
+  }
+  return true;
 }
 
 template <int NOD, bool KZERO>
@@ -779,6 +925,11 @@ HvArgs make_args(const Model& m, const Sector& s) {
   a.diag = s.d_diag.get(); a.diag32 = s.d_diag32.get();
   a.coefR = s.d_coefR.get(); a.coefR32 = s.d_coefR32.get();
   a.invR = s.d_invR.get(); a.invR32 = s.d_invR32.get();
+  a.uno = m.uni_no;
+  for (int k = 0; k < 2; ++k) {
+    a.uoff[k] = k < m.uni_no ? m.uni_off[k] : 0;
+    a.ubond[k] = k < m.uni_no ? m.uni_bond[k] : 0;
+  }
   return a;
 }
 
@@ -874,10 +1025,17 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
     check_launch("k_hv_u1_64");
   } else if (s.anchored) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
-    dispatch_nod(s.NOD, [&](auto c) {
-      if (s.kzero) k_hv_chain64<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
-      else k_hv_chain64<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
+    const bool uni = dispatch_uniform(m, s, [&](auto c, auto no) {
+      constexpr int N = decltype(c)::value, O = decltype(no)::value;
+      if (s.kzero) k_hv_uchain64<N, O, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      else k_hv_uchain64<N, O, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
     });
+    if (!uni) {
+      dispatch_nod(s.NOD, [&](auto c) {
+        if (s.kzero) k_hv_chain64<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y);
+        else k_hv_chain64<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y);
+      });
+    }
     check_launch("k_hv_chain64");
   } else {
     hv64_general(m, s, x, y, st);
@@ -893,10 +1051,15 @@ void hv64r(const Model& m, const Sector& s, const double* x, double* y, cudaStre
   const HvArgs a = make_args(m, s);
   const int pr = (pad && (s.D & 1)) ? 1 : 0;
   const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
-  dispatch_nod(s.NOD, [&](auto c) {
-    if (s.u1) k_hv_u1_64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
-    else k_hv_chain64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+  const bool uni = !s.u1 && dispatch_uniform(m, s, [&](auto c, auto no) {
+    k_hv_uchain64r<decltype(c)::value, decltype(no)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
   });
+  if (!uni) {
+    dispatch_nod(s.NOD, [&](auto c) {
+      if (s.u1) k_hv_u1_64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+      else k_hv_chain64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+    });
+  }
   check_launch("k_hv_real64");
 }
 
@@ -906,10 +1069,15 @@ void hv32r(const Model& m, const Sector& s, const float* x, float* y, cudaStream
   const HvArgs a = make_args(m, s);
   const int pr = (pad && (s.D & 1)) ? 1 : 0;
   const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
-  dispatch_nod(s.NOD, [&](auto c) {
-    if (s.u1) k_hv_u1_32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
-    else k_hv_chain32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
+  const bool uni = !s.u1 && dispatch_uniform(m, s, [&](auto c, auto no) {
+    k_hv_uchain32r<decltype(c)::value, decltype(no)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
   });
+  if (!uni) {
+    dispatch_nod(s.NOD, [&](auto c) {
+      if (s.u1) k_hv_u1_32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
+      else k_hv_chain32r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
+    });
+  }
   check_launch("k_hv_real32");
 }
 
@@ -968,10 +1136,17 @@ void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStrea
     check_launch("k_hv_u1_32");
   } else if (s.anchored) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
-    dispatch_nod(s.NOD, [&](auto c) {
-      if (s.kzero) k_hv_chain32<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
-      else k_hv_chain32<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+    const bool uni = dispatch_uniform(m, s, [&](auto c, auto no) {
+      constexpr int N = decltype(c)::value, O = decltype(no)::value;
+      if (s.kzero) k_hv_uchain32<N, O, true><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+      else k_hv_uchain32<N, O, false><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
     });
+    if (!uni) {
+      dispatch_nod(s.NOD, [&](auto c) {
+        if (s.kzero) k_hv_chain32<decltype(c)::value, true><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+        else k_hv_chain32<decltype(c)::value, false><<<grid, kHvThreads, 0, st>>>(a, x, y, shift);
+      });
+    }
     check_launch("k_hv_chain32");
   } else {
     const unsigned gw = (unsigned)((s.D * 32 + kHvThreads - 1) / kHvThreads);

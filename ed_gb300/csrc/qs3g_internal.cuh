@@ -92,6 +92,12 @@ struct Model {
   std::vector<int> adj_off;         // NOS + 2 (index by site 1..NOS, [NOS+1] end)
   std::vector<uint32_t> adj;        // packed (bond << 16) | neighbour  (NOS < 65536, bonds < 65536)
   std::vector<double> Sz_site;      // sum of sJz over the non-self bonds at a site (index 1..NOS)
+  // uniform chain: every site s has one bond to s + uni_off[k] (mod NOS) for
+  // k < uni_no, all bonds of a distance with the same couplings (uni_no = 0:
+  // not uniform); uni_bond[k] is one bond of distance uni_off[k]
+  int uni_no = 0;
+  int uni_off[2] = {0, 0};
+  int uni_bond[2] = {0, 0};
   // device copies
   DevBuf<int> d_adj_off;
   DevBuf<uint32_t> d_adj;
