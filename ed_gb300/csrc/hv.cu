@@ -68,6 +68,7 @@ struct HvArgs {
 };
 
 constexpr int kHvThreads = 256;
+constexpr int kUniBlocks = 5;  // uniform chain rows: 40 resident warps per SM (<= 51 registers)
 
 // ------------------------------------------------------------ chain kernels
 // One thread per row.  The row's diagonal is precomputed at sector build
@@ -270,6 +271,16 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   y[i] = row_out(di, xi, ir, ax, ay);
 }
 
+// The general hop out of line: the uniform rows unroll all their hops, and an
+// inlined copy of the general path per hop would crowd the instruction cache.
+// The row's configuration comes packed, so the caller's registers stay registers.
+template <int NOD>
+__device__ __noinline__ int chain_hop_slow(const HvArgs& a, uint64_t conf, int m, int e, int& ell, int& cnt) {
+  int n[NOD];
+  unpack<NOD>(conf, a.bits, n);
+  return chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+}
+
 // Uniform chains: every site s carries a bond to s + o (mod L) for each of NO
 // distances o < L/2, with one coupling per distance (the chains of the XXZ
 // configs).  The hops of spin m are then the moves by +o and -o: no
@@ -285,8 +296,9 @@ __device__ __forceinline__ void hv_uchain_row(const HvArgs& a, const V* __restri
                                               const typename Cplx<V>::R* __restrict__ invR,
                                               const typename Cplx<V>::P* __restrict__ ph, int64_t i, double shift) {
   using R = typename Cplx<V>::R;
+  const uint64_t cw = __ldg(a.conf + i);
   int n[NOD];
-  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  unpack<NOD>(cw, a.bits, n);
   int g[NOD];
 #pragma unroll
   for (int k = 0; k < NOD - 1; ++k) g[k] = n[k + 1] - n[k];
@@ -378,7 +390,7 @@ __device__ __forceinline__ void hv_uchain_row(const HvArgs& a, const V* __restri
 #pragma unroll
           for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
           if (edown) continue;  // parallel bond: diagonal only
-          id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+          id = chain_hop_slow<NOD>(a, cw, m, e, ell, cnt);
           cc = __ldg(coefR + a.ubond[k] * (NOD + 1) + cnt);
         }
         if (id < 0) continue;
@@ -393,7 +405,7 @@ __device__ __forceinline__ void hv_uchain_row(const HvArgs& a, const V* __restri
 }
 
 template <int NOD, int NO, bool KZERO>
-__global__ void __launch_bounds__(kHvThreads) k_hv_uchain64(HvArgs a, const double2* __restrict__ x,
+__global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain64(HvArgs a, const double2* __restrict__ x,
                                                             double2* __restrict__ y) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
@@ -401,7 +413,7 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_uchain64(HvArgs a, const doub
 }
 
 template <int NOD, int NO, bool KZERO>
-__global__ void __launch_bounds__(kHvThreads) k_hv_uchain32(HvArgs a, const float2* __restrict__ x,
+__global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain32(HvArgs a, const float2* __restrict__ x,
                                                             float2* __restrict__ y, float shift) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.D) return;
@@ -409,7 +421,7 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_uchain32(HvArgs a, const floa
 }
 
 template <int NOD, int NO>
-__global__ void __launch_bounds__(kHvThreads) k_hv_uchain64r(HvArgs a, const double* __restrict__ x,
+__global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain64r(HvArgs a, const double* __restrict__ x,
                                                              double* __restrict__ y, int pad) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.D) hv_uchain_row<NOD, NO, true, double>(a, x, y, a.diag, a.coefR, a.invR, nullptr, i, 0.0);
@@ -417,7 +429,7 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_uchain64r(HvArgs a, const dou
 }
 
 template <int NOD, int NO>
-__global__ void __launch_bounds__(kHvThreads) k_hv_uchain32r(HvArgs a, const float* __restrict__ x,
+__global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain32r(HvArgs a, const float* __restrict__ x,
                                                              float* __restrict__ y, float shift, int pad) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.D) hv_uchain_row<NOD, NO, true, float>(a, x, y, a.diag, a.coefR32, a.invR32, nullptr, i, (double)shift);
