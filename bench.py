@@ -279,6 +279,8 @@ def run_gpu(args, rank, world, local_rank, dist):
         line["gs_solve"] = solve_bench(args)
     if args.dsf and rank == 0:
         line["dsf_batch"] = dsf_bench()
+    if args.cfg5 and rank == 0 and world == 1:
+        line["cfg5_learned_start"] = cfg5_bench(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -477,6 +479,42 @@ def solve_bench(args):
     return out
 
 
+def cfg5_bench(args):
+    """The network's unseen test point (Delta = 0.7, J2 = 0.25: the Lifshitz
+    point of the magnon band, where the k = 0 level spacing falls as L^-4) at
+    L = 200 and L = 400, N_down = 4, k = 0: the learned start against the
+    random start, both precision 1 with real vectors, to ||r|| <= tol, each
+    solve stopped after --cfg5-limit seconds (reported, not converged)."""
+    from ed_gb300 import capi, learned
+    delta, j2 = 0.7, 0.25
+    net = capi.Mlp(seed=1)
+    learned.generate(net, learned.training_problems(seed=1))
+    learned.train(net, rounds=10, steps=300, batch=4096, lr=2e-3)
+    out = {"delta": delta, "J2": j2, "tol": args.tol, "NOK": args.nok, "NOM": args.nom,
+           "limit_s": args.cfg5_limit}
+    for L in (200, 400):
+        h = learned.chain_handle(L, delta, j2)
+        D = h.build_sector(NOD, (0, 0, 0))
+        v = learned.start_vector(net, h, delta, j2)
+        rec = {"sector_dim": D}
+        for name, start in (("learned", v), ("random", None)):
+            h.set_time_limit(args.cfg5_limit)
+            t0 = time.perf_counter()
+            r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=1 | capi.REAL,
+                        conv_mode=1, seed=7, start=start, want_psi=(name == "learned"), allow_unconverged=True)
+            dt = time.perf_counter() - t0
+            st = h.trlan_stats()
+            rec[name] = {"seconds": dt, "hv": r["iters"], "E0": float(r["ene"][0]), "resid": float(r["resid"][0]),
+                         "converged": bool(r["converged"]), "timed_out": st["timed_out"]}
+            if name == "learned":
+                psi = r["psi"][0]
+                rec["learned_start_overlap"] = float(abs(np.vdot(psi, v)) / np.linalg.norm(v) / np.linalg.norm(psi))
+        h.set_time_limit(0.0)
+        h.close()
+        out[f"L{L}"] = rec
+    return out
+
+
 def dsf_bench():
     """All q of a chain at once: L=200 Heisenberg ground state (N_down=3, k=0),
     S^-(q)|GS> in the N_down=4 sectors for q = 2 pi m / 200, m = 0..199, 150
@@ -528,6 +566,9 @@ def main():
     ap.add_argument("--solve-all", action="store_true",
                     help="with the solves, also the complex-vector, random-start and real FP64 arms")
     ap.add_argument("--dsf", action="store_true", help="add the all-q DSF batch (L=200, 200 q, 150 levels)")
+    ap.add_argument("--cfg5", action="store_true",
+                    help="add the learned-vs-random start comparison at (Delta, J2) = (0.7, 0.25), L = 200 and 400")
+    ap.add_argument("--cfg5-limit", type=float, default=300.0, help="wall seconds per --cfg5 solve")
     ap.add_argument("--nok", type=int, default=16)
     ap.add_argument("--nom", type=int, default=48)
     ap.add_argument("--maxrestart", type=int, default=40000)
