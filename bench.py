@@ -279,6 +279,8 @@ def run_gpu(args, rank, world, local_rank, dist):
         line["gs_solve"] = solve_bench(args)
     if args.dsf and rank == 0:
         line["dsf_batch"] = dsf_bench()
+    if args.batch and world == 1:
+        line["batched_solves"] = batch_bench(args)
     if args.cfg5 and rank == 0 and world == 1:
         line["cfg5_learned_start"] = cfg5_bench(args)
     if rank == 0:
@@ -515,6 +517,30 @@ def cfg5_bench(args):
     return out
 
 
+def batch_bench(args):
+    """The batched-solve workload: 256 XXZ chains from seed 1 (L in
+    {48..128}, N_down in {3, 4, 5}, k over the L momenta, Delta in [0, 2],
+    J2 in [0, 0.5]), lowest 2 eigenpairs each to ||r|| <= 1e-10 with FP32
+    Krylov vectors and FP64 reductions.  Both solvers from the same sectors:
+    qs3g_trlan_lockstep (all problems in one graph-replayed launch sequence)
+    and qs3g_trlan_batch (one stream per host thread, 8 threads)."""
+    from ed_gb300 import sweep
+    probs = sweep.random_chains(seed=1, n=args.batch_n)
+    out = {"workload": f"{args.batch_n}_random_xxz_chains_L48-128_Ndown3-5_lowest2_tol1e-10_fp32_vectors",
+           "NOE": 2, "NOK": 8, "NOM": 24}
+    for name, lock in (("lockstep", True), ("batch_8_streams", False)):
+        recs, tb, ts = sweep.solve(probs, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, lockstep=lock)
+        out[name] = {"solve_s": ts, "build_s": tb, "all_ok": all(r["status"] == 0 for r in recs),
+                     "max_resid": max(max(r["resid"]) for r in recs), "hv_total": sum(r["hv"] for r in recs)}
+        out.setdefault("rows_total", sum(r["D"] for r in recs))
+        out.setdefault("E0", [r["ene"][0] for r in recs])
+        if name == "batch_8_streams":
+            out["max_dE0_lockstep_vs_batch"] = max(abs(a - r["ene"][0]) for a, r in zip(out["E0"], recs))
+    out.pop("E0")
+    out["speedup_lockstep_vs_batch"] = out["batch_8_streams"]["solve_s"] / out["lockstep"]["solve_s"]
+    return out
+
+
 def dsf_bench():
     """All q of a chain at once: L=200 Heisenberg ground state (N_down=3, k=0),
     S^-(q)|GS> in the N_down=4 sectors for q = 2 pi m / 200, m = 0..199, 150
@@ -566,6 +592,9 @@ def main():
     ap.add_argument("--solve-all", action="store_true",
                     help="with the solves, also the complex-vector, random-start and real FP64 arms")
     ap.add_argument("--dsf", action="store_true", help="add the all-q DSF batch (L=200, 200 q, 150 levels)")
+    ap.add_argument("--batch", action="store_true",
+                    help="add the batched solves (256 random chains): lock step against concurrent streams")
+    ap.add_argument("--batch-n", type=int, default=256, help="problems in --batch")
     ap.add_argument("--cfg5", action="store_true",
                     help="add the learned-vs-random start comparison at (Delta, J2) = (0.7, 0.25), L = 200 and 400")
     ap.add_argument("--cfg5-limit", type=float, default=300.0, help="wall seconds per --cfg5 solve")

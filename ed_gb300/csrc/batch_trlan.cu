@@ -8,26 +8,26 @@
 // converged; a converged problem keeps its Ritz vectors in columns 0..NOE-1
 // and drops out of the maps at the next restart.  Per-problem scalars
 // (alpha, beta, overlaps, arrow couplings, Ritz coefficients) live in device
-// arrays indexed by problem; the small Ritz problems are solved on the host
-// for every active problem at each restart.  The steps and the convergence
+// arrays indexed by problem; the small Ritz problems are solved on the device
+// (k_britz, one block per active problem) and a whole restart cycle is
+// replayed as one CUDA graph.  The steps and the convergence
 // rule of each problem are those of trlan_core (krylov.cu); level-1
 // arithmetic is double-float on the FP32 pipe (eft.cuh) for both storage
 // types, so complex(4) phases keep FP64-accurate reductions.
 #include <algorithm>
 #include <cmath>
-#include <complex>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "eft.cuh"
-#include "hosteig.h"
 #include "krylov.h"
 #include "qs3g_internal.cuh"
 
 namespace qs3g {
 namespace {
 
-using zd = std::complex<double>;
 constexpr int kB = 256;          // rows per block
 constexpr int kChunkTiles = 16;  // overlap chunks: up to 16 blocks of one problem
 
@@ -59,27 +59,6 @@ __device__ __forceinline__ bool brow(const BSeg* segs, const int* bs, const int*
   const int64_t i = (int64_t)(blockIdx.x - bf[blockIdx.x]) * kB + threadIdx.x;
   r = segs[sg].row0 + i;
   return i < segs[sg].D;
-}
-
-// part[b] = sum over the block's rows of conj(x) y (double-float per thread)
-template <class T>
-__global__ void __launch_bounds__(kB) k_bdot(const BSeg* segs, const int* bs, const int* bf, const T* __restrict__ x,
-                                             const T* __restrict__ y, double2* part) {
-  __shared__ double2 sh[kB];
-  int64_t r;
-  int sg;
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  if (brow(segs, bs, bf, r, sg)) {
-    const float4 a = SplitLd<T>::ld(x[r]), b = SplitLd<T>::ld(y[r]);
-    const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
-    const float2 br = make_float2(b.x, b.y), bi = make_float2(b.z, b.w);
-    df_fma(rh, rl, ar, br);
-    df_fma(rh, rl, ai, bi);
-    df_fma(ih, il, ar, bi);
-    df_fma(ih, il, fneg2(ai), br);
-  }
-  const double2 s = block_sum2(make_double2(djoin(rh, rl), djoin(ih, il)), sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
 // One block per active problem: fixed-order sum of its blocks' partials.
@@ -225,12 +204,15 @@ __global__ void __launch_bounds__(kB) k_bgemv_final(const double2* part, int nch
   if (threadIdx.x == 0) ov[(size_t)sg * ldo + c] = s;
 }
 
-// w -= V[:, :ncols] * coef_s (coefficients of problem s at coef[s*ldo])
+// w -= V[:, :ncols] * coef_s (coefficients of problem s at coef[s*ldo]);
+// with npart set, also part[b] = sum |w|^2 of the stored result (k_bnrm's
+// partials, so the norm of the reorthogonalised vector needs no extra pass)
 template <class T>
 __global__ void __launch_bounds__(kB) k_bgemv_sub(const BSeg* segs, const int* bs, const int* bf,
                                                   const T* __restrict__ V, int64_t ldv, int ncols,
-                                                  const double2* __restrict__ coef, int ldo, T* w) {
+                                                  const double2* __restrict__ coef, int ldo, T* w, double2* npart) {
   __shared__ float4 c[128];
+  __shared__ double2 sh[kB];
   const int sg = bs[blockIdx.x];
   for (int k = threadIdx.x; k < ncols; k += kB) {
     const double2 ck = coef[(size_t)sg * ldo + k];
@@ -240,25 +222,37 @@ __global__ void __launch_bounds__(kB) k_bgemv_sub(const BSeg* segs, const int* b
   __syncthreads();
   int64_t r;
   int sg2;
-  if (!brow(segs, bs, bf, r, sg2)) return;
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  for (int k = 0; k < ncols; ++k) {
-    const float4 a = SplitLd<T>::ld(V[(int64_t)k * ldv + r]);
-    const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
-    const float4 ck = c[k];
-    const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
-    df_fma(rh, rl, cr, ar);
-    df_fma(rh, rl, fneg2(ci), ai);
-    df_fma(ih, il, cr, ai);
-    df_fma(ih, il, ci, ar);
+  float nh = 0.f, nl = 0.f;
+  if (brow(segs, bs, bf, r, sg2)) {
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int k = 0; k < ncols; ++k) {
+      const float4 a = SplitLd<T>::ld(V[(int64_t)k * ldv + r]);
+      const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+      const float4 ck = c[k];
+      const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
+      df_fma(rh, rl, cr, ar);
+      df_fma(rh, rl, fneg2(ci), ai);
+      df_fma(ih, il, cr, ai);
+      df_fma(ih, il, ci, ar);
+    }
+    const float4 wv = SplitLd<T>::ld(w[r]);
+    float wrh = wv.x, wrl = wv.y, wih = wv.z, wil = wv.w;
+    df_add(wrh, wrl, -rh);
+    wrl = __fsub_rn(wrl, rl);
+    df_add(wih, wil, -ih);
+    wil = __fsub_rn(wil, il);
+    const T out = Store<T>::st(wrh, wrl, wih, wil);
+    w[r] = out;
+    if (npart) {
+      const float4 a = SplitLd<T>::ld(out);
+      df_fma(nh, nl, make_float2(a.x, a.y), make_float2(a.x, a.y));
+      df_fma(nh, nl, make_float2(a.z, a.w), make_float2(a.z, a.w));
+    }
   }
-  const float4 wv = SplitLd<T>::ld(w[r]);
-  float wrh = wv.x, wrl = wv.y, wih = wv.z, wil = wv.w;
-  df_add(wrh, wrl, -rh);
-  wrl = __fsub_rn(wrl, rl);
-  df_add(wih, wil, -ih);
-  wil = __fsub_rn(wil, il);
-  w[r] = Store<T>::st(wrh, wrl, wih, wil);
+  if (npart) {
+    const double2 t = block_sum2(make_double2(djoin(nh, nl), 0.0), sh);
+    if (threadIdx.x == 0) npart[blockIdx.x] = t;
+  }
 }
 
 // In-place restart V[:, :nok] = V[:, :nom] C_s for the block's 256 rows, in
@@ -347,6 +341,249 @@ __global__ void k_bstart(const BSeg* segs, const int* bs, const int* bf, T* x, u
 
 unsigned sgrid(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
+// ------------------------------------------------------------------ device Ritz solves
+// One block per active problem, at the end of every Lanczos cycle: take the
+// cycle's alpha/beta into the problem's projected matrix -- tridiagonal after
+// the initial pass, arrowhead plus tridiagonal after a thick restart
+// (eigen_solver.f90:196-203) --, diagonalise it with a parallel cyclic Jacobi
+// method (round-robin pairs, each rotation herm_jacobi's), sort ascending,
+// and do trlan_core's restart bookkeeping on the device: the Ritz
+// coefficients C (NOM x NOK) for the next restart, the convergence test
+// (eigen_solver.f90:150-159, or the Ritz residual |beta_NOM C(NOM, j)|), the
+// retained Ritz values and the arrow couplings of the next cycle.  The host
+// only reads the per-problem flags.
+constexpr int kMaxRitz = 120;      // NOM limit of the lock-step batch
+constexpr int kRitzSmemMax = 80;   // above this the two NOM x NOM matrices live in global scratch
+
+struct RitzState {
+  int flag, stall, done, conv, tritr, brk;
+  double best;
+};
+
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 zaxpby(double2 a, double2 x, double2 b, double2 y) {
+  const double2 p = zmul(a, x), q = zmul(b, y);
+  return make_double2(p.x + q.x, p.y + q.y);
+}
+
+__global__ void __launch_bounds__(256) k_britz(const int* __restrict__ act, int first, int NOM, int NOK, int NOE,
+                                               int maxitr, double tol, int conv_mode, const double* __restrict__ shift,
+                                               const double2* __restrict__ alpha, const double2* __restrict__ beta,
+                                               double2* calpha, double2* cbeta, double2* C, double2* cb, double* ene,
+                                               RitzState* rs, int Ls, double2* scratch) {
+  extern __shared__ float4 smr[];  // same declaration as k_brestart's
+  const int n = NOM;
+  const int s = act[blockIdx.x];
+  // A: the projected matrix, Z: its eigenvectors (both n x n column-major)
+  double2* A = scratch ? scratch + (size_t)s * 2 * n * n : reinterpret_cast<double2*>(smr);
+  double2* Z = A + n * n;
+  __shared__ double w[kMaxRitz], red[256];
+  __shared__ int ord[kMaxRitz];
+  __shared__ int rp[kMaxRitz / 2], rq[kMaxRitz / 2];
+  __shared__ double rc[kMaxRitz / 2], rsn[kMaxRitz / 2];
+  __shared__ double2 rqp[kMaxRitz / 2], rqq[kMaxRitz / 2];
+  __shared__ int brk;
+  const int tid = threadIdx.x;
+  const double2* a = alpha + (size_t)s * Ls;
+  const double2* b = beta + (size_t)s * Ls;
+  double2* ca = calpha + (size_t)s * Ls;
+  double2* cbt = cbeta + (size_t)s * Ls;
+  if (tid == 0) brk = 0;
+  __syncthreads();
+  // 1. this cycle's scalars
+  if (first) {
+    for (int j = tid; j <= n; j += blockDim.x) {
+      if (j >= 1) ca[j] = make_double2(a[j].x, 0.0);
+      cbt[j] = make_double2(b[j].x, 0.0);
+      if (!(isfinite(b[j].x) && b[j].x > 0.0) || (j >= 1 && !isfinite(a[j].x))) brk = 1;
+    }
+  } else {
+    for (int j = NOK + 1 + tid; j <= n; j += blockDim.x) {
+      ca[j] = a[j];
+      cbt[j] = make_double2(b[j].x, 0.0);
+      if (!(isfinite(b[j].x) && b[j].x > 0.0) || !isfinite(a[j].x)) brk = 1;
+    }
+  }
+  __syncthreads();
+  if (brk) {
+    if (tid == 0) { rs[s].brk = 1; rs[s].done = 1; }
+    return;
+  }
+  // 2. the projected matrix (full Hermitian storage)
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    A[e] = make_double2(0.0, 0.0);
+    Z[e] = make_double2((e % n) == (e / n) ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    auto setu = [&](int i, int j, double2 v) {  // upper (i < j) and its conjugate
+      A[i + (size_t)j * n] = v;
+      A[j + (size_t)i * n] = zconj(v);
+    };
+    for (int j = 0; j < n; ++j) A[j + (size_t)j * n] = make_double2(ca[j + 1].x, 0.0);
+    if (first) {
+      for (int j = 0; j < n - 1; ++j) setu(j, j + 1, make_double2(b[j + 1].x, 0.0));
+    } else {
+      for (int j = 0; j < NOK; ++j) setu(j, NOK, cbt[j + 1]);
+      for (int j = NOK + 1; j <= n - 1; ++j) setu(j - 1, j, cbt[j]);
+    }
+  }
+  __syncthreads();
+  // 3. parallel cyclic Jacobi: m = n rounded up to even, m - 1 rounds of m / 2
+  //    disjoint pairs per sweep (circle method)
+  const int m = n + (n & 1);
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int e = tid; e < n * n; e += blockDim.x) {
+      const double a2 = A[e].x * A[e].x + A[e].y * A[e].y;
+      tot += a2;
+      if ((e % n) != (e / n)) off += a2;
+    }
+    red[tid] = off;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+      if (tid < h) red[tid] += red[tid + h];
+      __syncthreads();
+    }
+    const double offs = red[0];
+    __syncthreads();
+    red[tid] = tot;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+      if (tid < h) red[tid] += red[tid + h];
+      __syncthreads();
+    }
+    const double tots = red[0];
+    __syncthreads();
+    if (offs <= 1e-34 * tots || offs == 0.0) break;
+    for (int r = 0; r < m - 1; ++r) {
+      if (tid < m / 2) {
+        int p = (tid == 0) ? r : (r + tid) % (m - 1);
+        int q = (tid == 0) ? m - 1 : (r - tid + (m - 1)) % (m - 1);
+        if (p > q) { const int t = p; p = q; q = t; }
+        rp[tid] = p;
+        rq[tid] = q;
+        rc[tid] = 1.0;
+        rsn[tid] = 0.0;
+        rqp[tid] = make_double2(0.0, 0.0);
+        rqq[tid] = make_double2(1.0, 0.0);
+        if (q < n) {
+          const double2 apq = A[p + (size_t)q * n];
+          const double aa = sqrt(apq.x * apq.x + apq.y * apq.y);
+          if (aa != 0.0) {
+            const double app = A[p + (size_t)p * n].x, aqq = A[q + (size_t)q * n].x;
+            const double2 u = make_double2(apq.x / aa, apq.y / aa);
+            const double tau = (aqq - app) / (2.0 * aa);
+            const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            const double c = 1.0 / sqrt(1.0 + t * t), sn = t * c;
+            rc[tid] = c;
+            rsn[tid] = sn;
+            rqp[tid] = make_double2(-sn * u.x, sn * u.y);  // -s conj(u)
+            rqq[tid] = make_double2(c * u.x, -c * u.y);    //  c conj(u)
+          } else {
+            rq[tid] = n;  // no rotation
+          }
+        }
+      }
+      __syncthreads();
+      const int np = m / 2;
+      // columns: A <- A J, Z <- Z J
+      for (int it = tid; it < np * n; it += blockDim.x) {
+        const int k = it / n, i = it % n;
+        const int p = rp[k], q = rq[k];
+        if (q >= n) continue;
+        const double2 cc = make_double2(rc[k], 0.0), ss = make_double2(rsn[k], 0.0);
+        const double2 aip = A[i + (size_t)p * n], aiq = A[i + (size_t)q * n];
+        A[i + (size_t)p * n] = zaxpby(cc, aip, rqp[k], aiq);
+        A[i + (size_t)q * n] = zaxpby(ss, aip, rqq[k], aiq);
+        const double2 zip = Z[i + (size_t)p * n], ziq = Z[i + (size_t)q * n];
+        Z[i + (size_t)p * n] = zaxpby(cc, zip, rqp[k], ziq);
+        Z[i + (size_t)q * n] = zaxpby(ss, zip, rqq[k], ziq);
+      }
+      __syncthreads();
+      // rows: A <- J^H A
+      for (int it = tid; it < np * n; it += blockDim.x) {
+        const int k = it / n, i = it % n;
+        const int p = rp[k], q = rq[k];
+        if (q >= n) continue;
+        const double2 cc = make_double2(rc[k], 0.0), ss = make_double2(rsn[k], 0.0);
+        const double2 api = A[p + (size_t)i * n], aqi = A[q + (size_t)i * n];
+        A[p + (size_t)i * n] = zaxpby(cc, api, zconj(rqp[k]), aqi);
+        A[q + (size_t)i * n] = zaxpby(ss, api, zconj(rqq[k]), aqi);
+      }
+      __syncthreads();
+      if (tid < np) {
+        const int p = rp[tid], q = rq[tid];
+        if (q < n) {
+          A[p + (size_t)q * n] = make_double2(0.0, 0.0);
+          A[q + (size_t)p * n] = make_double2(0.0, 0.0);
+          A[p + (size_t)p * n].y = 0.0;
+          A[q + (size_t)q * n].y = 0.0;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // 4. ascending order
+  if (tid == 0) {
+    for (int i = 0; i < n; ++i) { w[i] = A[i + (size_t)i * n].x; ord[i] = i; }
+    for (int i = 1; i < n; ++i) {  // stable insertion sort of the indices
+      const int oi = ord[i];
+      int j = i - 1;
+      while (j >= 0 && w[ord[j]] > w[oi]) { ord[j + 1] = ord[j]; --j; }
+      ord[j + 1] = oi;
+    }
+  }
+  __syncthreads();
+  // 5. convergence (before the retained Ritz values overwrite calpha)
+  if (tid == 0) {
+    RitzState st = rs[s];
+    double mc = 0.0;
+    if (conv_mode == 0) {
+      for (int j = 0; j < NOK; ++j) mc = fmax(mc, fabs(ca[j + 1].x / w[ord[j]] - 1.0));
+    } else {
+      const double bN = cbt[n].x;
+      for (int j = 0; j < NOE; ++j) {
+        const double2 zl = Z[(n - 1) + (size_t)ord[j] * n];
+        double rj = fabs(bN) * sqrt(zl.x * zl.x + zl.y * zl.y);
+        if (conv_mode == 2) rj /= fmax(1.0, fabs(w[ord[j]] + shift[s]));
+        mc = fmax(mc, rj);
+      }
+    }
+    st.tritr += 1;  // one restart follows every Ritz solve
+    st.flag = (mc < tol) ? st.flag + 1 : 0;
+    if ((conv_mode == 0 && st.flag == 2) || (conv_mode != 0 && st.flag >= 1)) {
+      st.done = 1;
+      st.conv = 1;
+    } else if (conv_mode == 2) {
+      if (mc < 0.95 * st.best) { st.best = mc; st.stall = 0; }
+      else if (++st.stall >= 20) st.done = 1;
+    }
+    if (st.tritr >= maxitr) st.done = 1;
+    rs[s] = st;
+  }
+  __syncthreads();
+  // 6. Ritz values, coefficients for the restart, next cycle's retained scalars
+  for (int j = tid; j < n; j += blockDim.x) ene[(size_t)s * Ls + j] = w[ord[j]];
+  for (int e = tid; e < n * NOK; e += blockDim.x) {
+    const int j = e / n, i = e % n;
+    C[(size_t)s * n * NOK + (size_t)j * n + i] = Z[i + (size_t)ord[j] * n];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double2 bN = cbt[n];
+    for (int j = 0; j < NOK; ++j) ca[j + 1] = make_double2(w[ord[j]], 0.0);
+    for (int j = 1; j <= NOK; ++j) {
+      const double2 zl = Z[(n - 1) + (size_t)ord[j - 1] * n];
+      cbt[j] = zmul(bN, zl);
+      cb[(size_t)s * Ls + (j - 1)] = cbt[j];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ launch maps
 struct Maps {
   int nseg = 0, nact = 0, nblk = 0, nchunk = 0;
@@ -414,28 +651,60 @@ struct Maps {
   }
 };
 
-struct SegState {
-  std::vector<double> ene;
-  std::vector<zd> Cc, calpha, cbeta, Tm;
-  int flag = 0, stall = 0, hv = 0;
-  double best = 1e300;
-  bool done = false, converged = false;
+// Pinned host copy of the per-problem Ritz states (read once per cycle).
+struct PinnedStates {
+  RitzState* p = nullptr;
+  explicit PinnedStates(size_t n) { QS3G_CHECK_CUDA(cudaMallocHost((void**)&p, std::max<size_t>(1, n) * sizeof(RitzState))); }
+  ~PinnedStates() { if (p) cudaFreeHost(p); }
+  PinnedStates(const PinnedStates&) = delete;
+  PinnedStates& operator=(const PinnedStates&) = delete;
+};
+
+// One instantiated restart cycle; re-captured whenever the launch maps change.
+struct CycleGraph {
+  cudaGraphExec_t exec = nullptr;
+  ~CycleGraph() { reset(); }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
 };
 
 // Lock-step TRLan on the problems marked in `on`, from V[:,0] of each.
 // On return each problem's V[:, :NOE] holds its Ritz vectors, ene[s] its
 // Ritz values (shifted back), and conv[s] whether it met the test.
+//
+// Per cycle everything runs on the device: the Lanczos steps of all active
+// problems, k_britz (Ritz solve, convergence test, restart coefficients) and
+// k_brestart, followed by one copy of the Ritz states to pinned host memory.
+// A cycle is captured once into a CUDA graph and replayed until a problem
+// finishes; the host then drops it from the launch maps and captures again.
 template <class T>
-void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, const std::vector<int>& nod_of,
+void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, const DevBuf<HvSeg>& d_hs,
+                   const std::vector<int>& nod_of,
                    std::vector<char> on, T* V, int64_t ldv, T* Q, int NOE, int NOK, int NOM, int maxitr,
                    double tol, int conv_mode, const std::vector<double>& shift, std::vector<std::vector<double>>& ene,
                    std::vector<char>& conv, std::vector<int>& hv, cudaStream_t st) {
   const int n = (int)segs.size();
   const int64_t Ls = NOM + 2;  // per-problem stride of the scalar arrays
+  QS3G_REQUIRE(NOM <= kMaxRitz, QS3G_EINVAL, "NOM above the lock-step limit");
   DevBuf<BSeg> d_segs(n);
   QS3G_CHECK_CUDA(cudaMemcpyAsync(d_segs.get(), segs.data(), n * sizeof(BSeg), cudaMemcpyHostToDevice, st));
   DevBuf<double2> alpha((size_t)n * Ls), beta((size_t)n * Ls), ov((size_t)n * Ls), cb((size_t)n * Ls);
-  DevBuf<double2> C((size_t)n * NOM * NOK);
+  DevBuf<double2> calpha((size_t)n * Ls), cbeta((size_t)n * Ls), C((size_t)n * NOM * NOK);
+  DevBuf<double> d_ene((size_t)n * Ls), d_shift(n);
+  DevBuf<RitzState> d_rs(n);
+  QS3G_CHECK_CUDA(cudaMemsetAsync(C.get(), 0, C.n * sizeof(double2), st));
+  QS3G_CHECK_CUDA(cudaMemsetAsync(d_ene.get(), 0, d_ene.n * sizeof(double), st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_shift.get(), shift.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  PinnedStates h_rs(n);
+  for (int s = 0; s < n; ++s) h_rs.p[s] = RitzState{0, 0, 0, 0, 0, 0, 1e300};
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(d_rs.get(), h_rs.p, n * sizeof(RitzState), cudaMemcpyHostToDevice, st));
+  const bool ritz_smem = NOM <= kRitzSmemMax;
+  DevBuf<double2> ritz_scratch(ritz_smem ? 0 : (size_t)n * 2 * NOM * NOM);
+  const size_t ritz_sm = ritz_smem ? (size_t)2 * NOM * NOM * sizeof(double2) : 0;
+  if (ritz_smem)
+    QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_britz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ritz_sm));
   Maps mp;
   mp.nod_of = nod_of;
   mp.build(segs, on, st);
@@ -444,29 +713,67 @@ void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, con
   int64_t maxblk = 0;
   for (auto& s : segs) maxblk += (s.D + kB - 1) / kB;
   DevBuf<double2> part((size_t)std::max<int64_t>(maxblk, (int64_t)(NOM + 1) * maxchunk) + 1);
-  std::vector<SegState> S(n);
+  std::vector<int> hv_run(n, 0);
   auto col = [&](int j) { return V + (int64_t)j * ldv; };
   const BSeg* sg = d_segs.get();
 
-  auto hvop = [&](const T* x, T* y) {
-    for (int g = 1; g <= 8; ++g) {
-      if (mp.gnblk[g] == 0) continue;
-      if constexpr (sizeof(T) == sizeof(float2))
-        hv32_seg(g, d_hs.get(), mp.d_gbs[g].get(), mp.d_gbf[g].get(), mp.gnblk[g], reinterpret_cast<const float2*>(x),
-                 reinterpret_cast<float2*>(y), st);
-      else
-        hv64_seg(g, d_hs.get(), mp.d_gbs[g].get(), mp.d_gbf[g].get(), mp.gnblk[g], reinterpret_cast<const double2*>(x),
-                 reinterpret_cast<double2*>(y), 0.0, st);
-    }
-    for (int s : mp.active) ++S[s].hv;
-  };
   auto final_ = [&](double2* out, int mode) {
     k_bfinal<<<mp.nact, kB, 0, st>>>(part.get(), mp.d_sb0.get(), mp.d_snb.get(), mp.d_act.get(), out, Ls, mode);
     check_launch("k_bfinal");
   };
-  auto dot = [&](const T* x, const T* y, double2* out) {
-    k_bdot<T><<<mp.nblk, kB, 0, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), x, y, part.get());
-    check_launch("k_bdot");
+  // Row form per NOD group: a group whose chains are all uniform with the
+  // same number of bond distances can take the unrolled uniform row; the
+  // faster of the two on this batch's data is kept (QS3G_SEG_FORM=general or
+  // uniform pins the choice).
+  std::vector<int> seg_uni(9, 0);
+  auto hv_group = [&](int g, int uni, const T* x, T* y, double2* pp) {
+    if constexpr (sizeof(T) == sizeof(float2))
+      hv32_seg(g, d_hs.get(), mp.d_gbs[g].get(), mp.d_gbf[g].get(), mp.gnblk[g], reinterpret_cast<const float2*>(x),
+               reinterpret_cast<float2*>(y), st, pp, mp.d_sb0.get(), uni);
+    else
+      hv64_seg(g, d_hs.get(), mp.d_gbs[g].get(), mp.d_gbf[g].get(), mp.gnblk[g], reinterpret_cast<const double2*>(x),
+               reinterpret_cast<double2*>(y), 0.0, st, pp, mp.d_sb0.get(), uni);
+  };
+  {
+    const char* env = std::getenv("QS3G_SEG_FORM");
+    const std::string form = env ? env : "auto";
+    cudaEvent_t e0, e1;
+    QS3G_CHECK_CUDA(cudaEventCreate(&e0));
+    QS3G_CHECK_CUDA(cudaEventCreate(&e1));
+    for (int g = 1; g <= 8; ++g) {
+      if (mp.gnblk[g] == 0 || form == "general") continue;
+      int uno = -1;
+      for (int s : mp.active)
+        if (nod_of[s] == g) uno = (uno == -1 || uno == hs[s].uno) ? hs[s].uno : 0;
+      if (uno <= 0 || !seg_uniform_ok(g, uno)) continue;
+      if (form == "uniform") {
+        seg_uni[g] = uno;
+        continue;
+      }
+      float best[2] = {1e30f, 1e30f};
+      for (int rep = 0; rep < 3; ++rep)
+        for (int f = 0; f < 2; ++f) {
+          QS3G_CHECK_CUDA(cudaEventRecord(e0, st));
+          hv_group(g, f ? uno : 0, col(0), Q, part.get());
+          QS3G_CHECK_CUDA(cudaEventRecord(e1, st));
+          QS3G_CHECK_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          QS3G_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (rep > 0) best[f] = std::min(best[f], ms);  // rep 0 warms up
+        }
+      seg_uni[g] = best[1] < best[0] ? uno : 0;
+      if (verbose())
+        std::printf("batched trlan: NOD %d group, general %.3f ms, uniform %.3f ms -> %s\n", g, best[0], best[1],
+                    seg_uni[g] ? "uniform" : "general");
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  // y = H x for every active problem, with alpha = <x, y> reduced from the
+  // H*v kernels' own block partials
+  auto hvdot = [&](const T* x, T* y, double2* out) {
+    for (int g = 1; g <= 8; ++g)
+      if (mp.gnblk[g]) hv_group(g, seg_uni[g], x, y, part.get());
     final_(out, 0);
   };
   auto nrm = [&](const T* x, double2* out) {
@@ -483,13 +790,17 @@ void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, con
                                              real_alpha ? 1 : 0);
     check_launch("k_blanczos_w");
   };
-  auto gsub = [&](int ncols, const double2* coef, T* w) {
-    k_bgemv_sub<T><<<mp.nblk, kB, 0, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), V, ldv, ncols, coef, (int)Ls, w);
+  auto gsub = [&](int ncols, const double2* coef, T* w, double2* npart) {
+    k_bgemv_sub<T><<<mp.nblk, kB, 0, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), V, ldv, ncols, coef, (int)Ls, w, npart);
     check_launch("k_bgemv_sub");
   };
-  auto reorth = [&](int i) {  // against columns 0..i-2
+  // column i against columns 0..i-2, then beta_i = ||column i||
+  auto reorth_nrm = [&](int i) {
     const int ncols = i - 1;
-    if (ncols <= 0) return;
+    if (ncols <= 0) {
+      nrm(col(i), beta.get() + i);
+      return;
+    }
     k_bgemv_h<T><<<dim3((unsigned)((ncols + 3) / 4), (unsigned)mp.nchunk), kB, 0, st>>>(V, ldv, ncols, col(i),
                                                                                         mp.d_chunks.get(), part.get());
     check_launch("k_bgemv_h");
@@ -497,136 +808,105 @@ void lockstep_core(const std::vector<BSeg>& segs, const DevBuf<HvSeg>& d_hs, con
                                                                          mp.d_snc.get(), mp.d_act.get(), ov.get(),
                                                                          (int)Ls);
     check_launch("k_bgemv_final");
-    gsub(ncols, ov.get(), col(i));
+    gsub(ncols, ov.get(), col(i), part.get());
+    final_(beta.get() + i, 1);
   };
   const size_t rsm = ((size_t)NOM * NOK + (size_t)NOM * 32) * sizeof(float4);
   QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_brestart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
-  std::vector<double2> ha((size_t)n * Ls), hb((size_t)n * Ls);
-  auto fetch = [&]() {
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(ha.data(), alpha.get(), ha.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(hb.data(), beta.get(), hb.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  // Ritz solve + test, restart, the next cycle's first column, states to the host
+  auto close_cycle = [&](int first) {
+    scale(col(NOM), beta.get() + NOM);
+    k_britz<<<mp.nact, 256, ritz_sm, st>>>(mp.d_act.get(), first, NOM, NOK, NOE, maxitr, tol, conv_mode,
+                                           d_shift.get(), alpha.get(), beta.get(), calpha.get(), cbeta.get(), C.get(),
+                                           cb.get(), d_ene.get(), d_rs.get(), (int)Ls, ritz_scratch.get());
+    check_launch("k_britz");
+    k_brestart<T><<<mp.nblk, kB, rsm, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), V, ldv, NOM, NOK, C.get());
+    check_launch("k_brestart");
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(col(NOK), col(NOM), ldv * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(h_rs.p, d_rs.get(), n * sizeof(RitzState), cudaMemcpyDeviceToHost, st));
+  };
+  auto restart_cycle = [&]() {
+    int i = NOK + 1;
+    hvdot(col(i - 1), Q, alpha.get() + i);
+    gsub(NOK, cb.get(), Q, nullptr);
+    lw(col(i), Q, col(i - 1), nullptr, alpha.get() + i, beta.get(), false);
+    reorth_nrm(i);
+    for (i = NOK + 2; i <= NOM; ++i) {
+      scale(col(i - 1), beta.get() + (i - 1));
+      hvdot(col(i - 1), Q, alpha.get() + i);
+      lw(col(i), Q, col(i - 1), col(i - 2), alpha.get() + i, beta.get() + (i - 1), false);
+      reorth_nrm(i);
+    }
+    close_cycle(0);
+  };
+  // read the states of the cycle just run; true when the active set changed
+  auto settle = [&](int nhv) {
     QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
+    bool changed = false;
+    for (int s : mp.active) {
+      hv_run[s] += nhv;
+      QS3G_REQUIRE(!h_rs.p[s].brk, QS3G_EBREAKDOWN, "Lanczos breakdown in a batched problem");
+      if (h_rs.p[s].done) {
+        on[s] = 0;
+        changed = true;
+      }
+    }
+    return changed;
+  };
+  const bool can_capture = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+  CycleGraph graph;
+  auto capture = [&]() {
+    graph.reset();
+    if (!can_capture) return;
+    cudaGraph_t g = nullptr;
+    QS3G_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      restart_cycle();
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      throw;
+    }
+    QS3G_CHECK_CUDA(cudaStreamEndCapture(st, &g));
+    const cudaError_t e = cudaGraphInstantiate(&graph.exec, g, 0);
+    cudaGraphDestroy(g);
+    QS3G_CHECK_CUDA(e);
   };
 
   // ---- initial Lanczos pass
   nrm(col(0), beta.get());
   for (int i = 1; i <= NOM; ++i) {
     scale(col(i - 1), beta.get() + (i - 1));
-    hvop(col(i - 1), Q);
-    dot(col(i - 1), Q, alpha.get() + i);
-    if (i > 1) {
-      lw(col(i), Q, col(i - 1), col(i - 2), alpha.get() + i, beta.get() + (i - 1), true);
-      reorth(i);
-    } else {
-      lw(col(i), Q, col(i - 1), nullptr, alpha.get() + i, beta.get(), true);
-    }
-    nrm(col(i), beta.get() + i);
+    hvdot(col(i - 1), Q, alpha.get() + i);
+    if (i > 1) lw(col(i), Q, col(i - 1), col(i - 2), alpha.get() + i, beta.get() + (i - 1), true);
+    else lw(col(i), Q, col(i - 1), nullptr, alpha.get() + i, beta.get(), true);
+    reorth_nrm(i);
   }
-  scale(col(NOM), beta.get() + NOM);
-  fetch();
-  for (int s : mp.active) {
-    SegState& x = S[s];
-    const double2* a = ha.data() + s * Ls;
-    const double2* b = hb.data() + s * Ls;
-    for (int i = 0; i <= NOM; ++i)
-      QS3G_REQUIRE(std::isfinite(b[i].x) && b[i].x > 0.0 && std::isfinite(a[i < 1 ? 1 : i].x), QS3G_EBREAKDOWN,
-                   "Lanczos breakdown in the initial pass of a batched problem");
-    x.Tm.assign((size_t)NOM * NOM, zd(0.0, 0.0));
-    for (int j = 0; j < NOM; ++j) x.Tm[j + (size_t)j * NOM] = a[j + 1].x;
-    for (int j = 0; j < NOM - 1; ++j) x.Tm[j + (size_t)(j + 1) * NOM] = b[j + 1].x;
-    herm_jacobi(NOM, x.Tm, x.ene, x.Cc);
-    x.calpha.assign(NOM + 1, 0.0);
-    x.cbeta.assign(NOM + 1, 0.0);
-    for (int j = 1; j <= NOM; ++j) x.calpha[j] = a[j].x;
-    for (int j = 0; j <= NOM; ++j) x.cbeta[j] = b[j].x;
+  close_cycle(1);
+  bool changed = settle(NOM);
+  for (int cycle = 0; cycle < maxitr && mp.nact > 0; ++cycle) {
+    if (changed) {
+      mp.build(segs, on, st);
+      if (mp.nact == 0) break;
+      graph.reset();
+    }
+    if (verbose()) std::printf("batched trlan: cycle %d, %d of %d problems active\n", cycle + 1, mp.nact, n);
+    if (can_capture && !graph.exec) capture();
+    if (graph.exec) QS3G_CHECK_CUDA(cudaGraphLaunch(graph.exec, st));
+    else restart_cycle();
+    changed = settle(NOM - NOK);
   }
-  std::vector<double2> hC((size_t)n * NOM * NOK), hcb((size_t)n * Ls);
-  for (int tritr = 1; tritr <= maxitr; ++tritr) {
-    for (int s : mp.active)
-      for (int j = 0; j < NOK; ++j)
-        for (int i = 0; i < NOM; ++i) {
-          const zd c = S[s].Cc[i + (size_t)j * NOM];
-          hC[(size_t)s * NOM * NOK + (size_t)j * NOM + i] = make_double2(c.real(), c.imag());
-        }
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(C.get(), hC.data(), hC.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
-    k_brestart<T><<<mp.nblk, kB, rsm, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), V, ldv, NOM, NOK, C.get());
-    check_launch("k_brestart");
-    // convergence per problem (trlan_core's rule)
-    bool changed = false;
-    for (int s : mp.active) {
-      SegState& x = S[s];
-      double mc = 0.0;
-      if (conv_mode == 0) {
-        for (int j = 0; j < NOK; ++j) mc = std::max(mc, std::abs(x.calpha[j + 1] / x.ene[j] - 1.0));
-      } else {
-        for (int j = 0; j < NOE; ++j) {
-          double rj = std::abs(x.cbeta[NOM] * x.Cc[(NOM - 1) + (size_t)j * NOM]);
-          if (conv_mode == 2) rj /= std::max(1.0, std::fabs(x.ene[j] + shift[s]));
-          mc = std::max(mc, rj);
-        }
-      }
-      x.flag = (mc < tol) ? x.flag + 1 : 0;
-      if ((conv_mode == 0 && x.flag == 2) || (conv_mode != 0 && x.flag >= 1)) {
-        x.done = x.converged = true;
-      } else if (conv_mode == 2) {
-        if (mc < 0.95 * x.best) { x.best = mc; x.stall = 0; }
-        else if (++x.stall >= 20) x.done = true;
-      }
-      if (tritr == maxitr) x.done = true;
-      if (x.done) { on[s] = 0; changed = true; }
-    }
-    if (verbose())
-      std::printf("batched trlan: restart %d, %d of %d problems active\n", tritr, mp.nact, n);
-    if (changed) mp.build(segs, on, st);
-    if (mp.nact == 0) break;
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(col(NOK), col(NOM), ldv * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    for (int s : mp.active) {
-      SegState& x = S[s];
-      for (int j = 0; j < NOK; ++j) x.calpha[j + 1] = x.ene[j];
-      for (int j = 1; j <= NOK; ++j) x.cbeta[j] = x.cbeta[NOM] * x.Cc[(NOM - 1) + (size_t)(j - 1) * NOM];
-      for (int j = 0; j < NOK; ++j) hcb[(size_t)s * Ls + j] = make_double2(x.cbeta[j + 1].real(), x.cbeta[j + 1].imag());
-    }
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(cb.get(), hcb.data(), hcb.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
-    int i = NOK + 1;
-    hvop(col(i - 1), Q);
-    dot(col(i - 1), Q, alpha.get() + i);
-    gsub(NOK, cb.get(), Q);
-    lw(col(i), Q, col(i - 1), nullptr, alpha.get() + i, beta.get(), false);
-    reorth(i);
-    nrm(col(i), beta.get() + i);
-    for (i = NOK + 2; i <= NOM; ++i) {
-      scale(col(i - 1), beta.get() + (i - 1));
-      hvop(col(i - 1), Q);
-      dot(col(i - 1), Q, alpha.get() + i);
-      lw(col(i), Q, col(i - 1), col(i - 2), alpha.get() + i, beta.get() + (i - 1), false);
-      reorth(i);
-      nrm(col(i), beta.get() + i);
-    }
-    scale(col(NOM), beta.get() + NOM);
-    fetch();
-    for (int s : mp.active) {
-      SegState& x = S[s];
-      const double2* a = ha.data() + s * Ls;
-      const double2* b = hb.data() + s * Ls;
-      for (int j = NOK + 1; j <= NOM; ++j) {
-        x.calpha[j] = zd(a[j].x, a[j].y);
-        x.cbeta[j] = b[j].x;
-        QS3G_REQUIRE(std::isfinite(b[j].x) && b[j].x > 0.0 && std::isfinite(a[j].x), QS3G_EBREAKDOWN,
-                     "Lanczos breakdown after a restart of a batched problem");
-      }
-      std::fill(x.Tm.begin(), x.Tm.end(), zd(0.0, 0.0));
-      for (int j = 0; j < NOM; ++j) x.Tm[j + (size_t)j * NOM] = x.calpha[j + 1];
-      for (int j = 0; j < NOK; ++j) x.Tm[j + (size_t)NOK * NOM] = x.cbeta[j + 1];
-      for (int j = NOK + 1; j <= NOM - 1; ++j) x.Tm[(j - 1) + (size_t)j * NOM] = x.cbeta[j];
-      herm_jacobi(NOM, x.Tm, x.ene, x.Cc);
-    }
-  }
+  std::vector<double> he((size_t)n * Ls);
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(he.data(), d_ene.get(), he.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaMemcpyAsync(h_rs.p, d_rs.get(), n * sizeof(RitzState), cudaMemcpyDeviceToHost, st));
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
   for (int s = 0; s < n; ++s) {
-    if (S[s].ene.empty()) continue;  // not part of this run
-    ene[s].assign(S[s].ene.begin(), S[s].ene.begin() + NOE);
+    if (h_rs.p[s].tritr == 0) continue;  // not part of this run
+    ene[s].assign(he.begin() + (size_t)s * Ls, he.begin() + (size_t)s * Ls + NOE);
     for (double& e : ene[s]) e += shift[s];
-    conv[s] = S[s].converged ? 1 : 0;
-    hv[s] += S[s].hv;
+    conv[s] = h_rs.p[s].conv ? 1 : 0;
+    hv[s] += hv_run[s];
   }
 }
 
@@ -678,7 +958,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
     k_bstart<float2><<<all.nblk, kB, 0, st>>>(d_segs.get(), all.d_bs.get(), all.d_bf.get(), V32.get(), p.seed);
     check_launch("k_bstart");
     const double tol1 = phase1_tol(p.tol32);
-    lockstep_core<float2>(segs, d_hs, nod_of, on, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, shift,
+    lockstep_core<float2>(segs, hs, d_hs, nod_of, on, V32.get(), ldv, Q32.get(), NOE, NOK, NOM, p.maxitr, tol1, 2, shift,
                           ene, conv, hv, st);
     // phase 2 start: the sum of the NOE Ritz vectors, widened to FP64
     k_bto64<<<sgrid(ldv), 256, 0, st>>>(V64.get(), V32.get(), ldv);
@@ -707,7 +987,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
   DevBuf<double2> d_r((size_t)std::max(1, n) * 1);
   for (int attempt = 0; attempt < 4; ++attempt) {
     std::fill(conv.begin(), conv.end(), 0);
-    lockstep_core<double2>(segs, d_hs, nod_of, todo, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est,
+    lockstep_core<double2>(segs, hs, d_hs, nod_of, todo, V64.get(), ldv, Q64.get(), NOE, NOK, NOM, p.maxitr, tol_est,
                            p.conv_mode, zero, ene, conv, hv, st);
     if (p.conv_mode == 0) break;
     // residual of every Ritz pair of the problems just solved
@@ -765,7 +1045,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
       // V[:,0] -= (-1) * V[:,j]  (one column through the batched subtraction)
       k_bgemv_sub<double2><<<mp2.nblk, kB, 0, st>>>(d_segs.get(), mp2.d_bs.get(), mp2.d_bf.get(),
                                                     V64.get() + (int64_t)j * ldv, ldv, 1, cone.get(), NOM + 2,
-                                                    V64.get());
+                                                    V64.get(), nullptr);
       check_launch("k_bgemv_sub");
       QS3G_CHECK_CUDA(cudaStreamSynchronize(st));
     }

@@ -15,6 +15,7 @@
 // all translations with the 32 lanes of a warp and reduce with shuffles.
 // The row index comes from the sector directory (one 32-byte load) instead of
 // findstate's binary search.
+#include "eft.cuh"
 #include "qs3g_device.cuh"
 #include "qs3g_internal.cuh"
 #include "krylov.h"
@@ -412,13 +413,6 @@ __global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain32(HvArgs a
   hv_uchain_row<NOD, NO, KZERO, float2>(a, x, y, a.diag, a.coefR32, a.invR32, a.chainph32, i, (double)shift);
 }
 
-template <int NOD, int NO>
-__global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain64r(HvArgs a, const double* __restrict__ x,
-                                                             double* __restrict__ y, int pad) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.D) hv_uchain_row<NOD, NO, true, double>(a, x, y, a.diag, a.coefR, a.invR, nullptr, i, 0.0);
-  else if (i == a.D && pad) y[i] = 0.0;
-}
 
 template <int NOD, int NO>
 __global__ void __launch_bounds__(kHvThreads, kUniBlocks) k_hv_uchain32r(HvArgs a, const float* __restrict__ x,
@@ -485,42 +479,99 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain32r(HvArgs a, const floa
 // ------------------------------------------------------------ batches of chain sectors
 // Block b works on segment blk_seg[b], rows (b - blk_first[b]) * 256 + tid of
 // it; the segment's tables replace the handle's in the row function.
-template <int NOD>
+// Batched chain products, optionally with the Lanczos alpha partials in the
+// epilogue: when part is set, block b also writes sum over its rows of
+// conj(x_i) y_i (double-float, k_bdot's order) to part[seg_b0[s] + local
+// block], the slot the separate dot kernel of batch_trlan.cu would fill.
+template <int NOD, int NO, class V>
+__device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const int* __restrict__ blk_seg,
+                                        const int* __restrict__ blk_first, const V* __restrict__ x, V* __restrict__ y,
+                                        double shift, double2* part, const int* __restrict__ seg_b0) {
+  __shared__ double2 sh[kHvThreads];
+  const int sg = blk_seg[blockIdx.x];
+  const HvSeg& g = segs[sg];
+  const int lb = blockIdx.x - blk_first[blockIdx.x];
+  const int64_t i = (int64_t)lb * blockDim.x + threadIdx.x;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  if (i < g.D) {
+    HvArgs a{};
+    a.D = g.D; a.L = g.L; a.NOS = g.L; a.bits = g.bits;
+    a.conf = g.conf; a.dir = g.dir; a.binomA = g.binomA; a.adj_off = g.adj_off; a.adj = g.adj;
+    const V* xs = x + g.row0;
+    V* ys = y + g.row0;
+    constexpr bool F64 = sizeof(V) == sizeof(double2);
+    const double sh_ = F64 ? shift : g.shift;
+    const auto* cR = [&] { if constexpr (F64) return g.coefR; else return g.coefR32; }();
+    const auto* iR = [&] { if constexpr (F64) return g.invR; else return g.invR32; }();
+    const auto* ph = [&] { if constexpr (F64) return g.chainph; else return g.chainph32; }();
+    if constexpr (NO == 0) {
+      if (g.kzero) hv_chain_row<NOD, true, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+      else hv_chain_row<NOD, false, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+    } else {
+      a.uno = NO;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        a.uoff[k] = g.uoff[k];
+        a.ubond[k] = g.ubond[k];
+      }
+      if (g.kzero) hv_uchain_row<NOD, NO, true, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+      else hv_uchain_row<NOD, NO, false, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+    }
+    if (part) {
+      const float4 u = SplitLd<V>::ld(xs[i]), v = SplitLd<V>::ld(ys[i]);
+      const float2 ur = make_float2(u.x, u.y), ui = make_float2(u.z, u.w);
+      const float2 vr = make_float2(v.x, v.y), vi = make_float2(v.z, v.w);
+      df_fma(rh, rl, ur, vr);
+      df_fma(rh, rl, ui, vi);
+      df_fma(ih, il, ur, vi);
+      df_fma(ih, il, fneg2(ui), vr);
+    }
+  }
+  if (part) {  // uniform across the block
+    const double2 t = block_sum2(make_double2(djoin(rh, rl), djoin(ih, il)), sh);
+    if (threadIdx.x == 0) part[seg_b0[sg] + lb] = t;
+  }
+}
+
+template <int NOD, int NO>
 __global__ void __launch_bounds__(kHvThreads) k_hv_chain64_seg(const HvSeg* __restrict__ segs,
                                                                const int* __restrict__ blk_seg,
                                                                const int* __restrict__ blk_first,
                                                                const double2* __restrict__ x,
-                                                               double2* __restrict__ y, double shift) {
-  const int sg = blk_seg[blockIdx.x];
-  const HvSeg& g = segs[sg];
-  const int64_t i = (int64_t)(blockIdx.x - blk_first[blockIdx.x]) * blockDim.x + threadIdx.x;
-  if (i >= g.D) return;
-  HvArgs a{};
-  a.D = g.D; a.L = g.L; a.NOS = g.L; a.bits = g.bits;
-  a.conf = g.conf; a.dir = g.dir; a.binomA = g.binomA; a.adj_off = g.adj_off; a.adj = g.adj;
-  const double2* xs = x + g.row0;
-  double2* ys = y + g.row0;
-  if (g.kzero) hv_chain_row<NOD, true, double2>(a, xs, ys, g.diag, g.coefR, g.invR, g.chainph, i, shift);
-  else hv_chain_row<NOD, false, double2>(a, xs, ys, g.diag, g.coefR, g.invR, g.chainph, i, shift);
+                                                               double2* __restrict__ y, double shift, double2* part,
+                                                               const int* __restrict__ seg_b0) {
+  seg_row<NOD, NO, double2>(segs, blk_seg, blk_first, x, y, shift, part, seg_b0);
 }
 
-template <int NOD>
+template <int NOD, int NO>
 __global__ void __launch_bounds__(kHvThreads) k_hv_chain32_seg(const HvSeg* __restrict__ segs,
                                                                const int* __restrict__ blk_seg,
                                                                const int* __restrict__ blk_first,
                                                                const float2* __restrict__ x,
-                                                               float2* __restrict__ y) {
-  const int sg = blk_seg[blockIdx.x];
-  const HvSeg& g = segs[sg];
-  const int64_t i = (int64_t)(blockIdx.x - blk_first[blockIdx.x]) * blockDim.x + threadIdx.x;
-  if (i >= g.D) return;
-  HvArgs a{};
-  a.D = g.D; a.L = g.L; a.NOS = g.L; a.bits = g.bits;
-  a.conf = g.conf; a.dir = g.dir; a.binomA = g.binomA; a.adj_off = g.adj_off; a.adj = g.adj;
-  const float2* xs = x + g.row0;
-  float2* ys = y + g.row0;
-  if (g.kzero) hv_chain_row<NOD, true, float2>(a, xs, ys, g.diag, g.coefR32, g.invR32, g.chainph32, i, g.shift);
-  else hv_chain_row<NOD, false, float2>(a, xs, ys, g.diag, g.coefR32, g.invR32, g.chainph32, i, g.shift);
+                                                               float2* __restrict__ y, double2* part,
+                                                               const int* __restrict__ seg_b0) {
+  seg_row<NOD, NO, float2>(segs, blk_seg, blk_first, x, y, 0.0, part, seg_b0);
+}
+
+// (NOD, uniform distances) -> f(nod, no) with compile-time constants; no = 0
+// is the general row, uniform forms for NOD 2..6
+template <class F>
+void dispatch_seg(int NOD, int uni, F&& f) {
+  if (uni >= 1 && uni <= 2 && NOD >= 2 && NOD <= 6) {
+    auto with_no = [&](auto nod) {
+      if (uni == 1) f(nod, std::integral_constant<int, 1>{});
+      else f(nod, std::integral_constant<int, 2>{});
+    };
+    switch (NOD) {
+      case 2: with_no(std::integral_constant<int, 2>{}); break;
+      case 3: with_no(std::integral_constant<int, 3>{}); break;
+      case 4: with_no(std::integral_constant<int, 4>{}); break;
+      case 5: with_no(std::integral_constant<int, 5>{}); break;
+      default: with_no(std::integral_constant<int, 6>{}); break;
+    }
+    return;
+  }
+  dispatch_nod(NOD, [&](auto c) { f(c, std::integral_constant<int, 0>{}); });
 }
 
 // ------------------------------------------------------------ U(1)-only kernels
@@ -975,23 +1026,33 @@ HvSeg make_seg(const Model& m, const Sector& s, int64_t row0) {
   g.diag32 = s.d_diag32.get(); g.coefR32 = s.d_coefR32.get(); g.invR32 = s.d_invR32.get();
   g.chainph32 = s.d_chainph32.get();
   g.shift = 0.0;
+  g.uno = m.uni_no;
+  for (int k = 0; k < 2; ++k) {
+    g.uoff[k] = k < m.uni_no ? m.uni_off[k] : 0;
+    g.ubond[k] = k < m.uni_no ? m.uni_bond[k] : 0;
+  }
   return g;
 }
 
+bool seg_uniform_ok(int NOD, int uni) { return uni >= 1 && uni <= 2 && NOD >= 2 && NOD <= 6; }
+
 void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
-              const float2* x, float2* y, cudaStream_t st) {
+              const float2* x, float2* y, cudaStream_t st, double2* part, const int* seg_b0, int uni) {
   if (nblk == 0) return;
-  dispatch_nod(NOD, [&](auto c) {
-    k_hv_chain32_seg<decltype(c)::value><<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y);
+  dispatch_seg(NOD, uni, [&](auto c, auto no) {
+    k_hv_chain32_seg<decltype(c)::value, decltype(no)::value>
+        <<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y, part, seg_b0);
   });
   check_launch("k_hv_chain32_seg");
 }
 
 void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
-              const double2* x, double2* y, double shift, cudaStream_t st) {
+              const double2* x, double2* y, double shift, cudaStream_t st, double2* part, const int* seg_b0,
+              int uni) {
   if (nblk == 0) return;
-  dispatch_nod(NOD, [&](auto c) {
-    k_hv_chain64_seg<decltype(c)::value><<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y, shift);
+  dispatch_seg(NOD, uni, [&](auto c, auto no) {
+    k_hv_chain64_seg<decltype(c)::value, decltype(no)::value>
+        <<<nblk, kHvThreads, 0, st>>>(d_segs, d_blk_seg, d_blk_first, x, y, shift, part, seg_b0);
   });
   check_launch("k_hv_chain64_seg");
 }
@@ -1051,15 +1112,12 @@ void hv64r(const Model& m, const Sector& s, const double* x, double* y, cudaStre
   const HvArgs a = make_args(m, s);
   const int pr = (pad && (s.D & 1)) ? 1 : 0;
   const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
-  const bool uni = !s.u1 && dispatch_uniform(m, s, [&](auto c, auto no) {
-    k_hv_uchain64r<decltype(c)::value, decltype(no)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+  // the general chain row, as the complex(8) product uses: the real product
+  // stays the real part of the complex one bit for bit
+  dispatch_nod(s.NOD, [&](auto c) {
+    if (s.u1) k_hv_u1_64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
+    else k_hv_chain64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
   });
-  if (!uni) {
-    dispatch_nod(s.NOD, [&](auto c) {
-      if (s.u1) k_hv_u1_64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
-      else k_hv_chain64r<decltype(c)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, pr);
-    });
-  }
   check_launch("k_hv_real64");
 }
 

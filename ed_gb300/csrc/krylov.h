@@ -67,18 +67,28 @@ struct HvSeg {
   const float* invR32;
   const float2* chainph32;
   double shift;             // per-sector shift of the complex(4) product (H - shift)
+  int uno;                  // uniform chain: number of bond distances (0: not uniform)
+  int uoff[2], ubond[2];    //   the distances and one bond of each
 };
 
 HvSeg make_seg(const Model& m, const Sector& s, int64_t row0);
 
 // H*v - shift*v over a batch of chain sectors with the same NOD: one launch,
 // block b serves segment blk_seg[b] (blocks of 256 rows, each segment padded
-// to whole blocks).
+// to whole blocks).  With part set, block b also stores its rows' share of
+// <x, y> at part[seg_b0[segment] + b - blk_first[b]].
+// uni = 1 or 2: every segment of the launch is a uniform chain with that many
+// bond distances, and the rows take hv_uchain_row's unrolled form (the same
+// hops summed in another order); uni = 0: the general chain row.
 void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
-              const double2* x, double2* y, double shift, cudaStream_t st);
+              const double2* x, double2* y, double shift, cudaStream_t st, double2* part = nullptr,
+              const int* seg_b0 = nullptr, int uni = 0);
 // complex(4) form: every segment applies H - its own shift
 void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
-              const float2* x, float2* y, cudaStream_t st);
+              const float2* x, float2* y, cudaStream_t st, double2* part = nullptr, const int* seg_b0 = nullptr,
+              int uni = 0);
+// true when the uniform form exists for NOD and uni
+bool seg_uniform_ok(int NOD, int uni);
 
 
 struct TrlanParams {

@@ -41,3 +41,19 @@ def test_trlan_lockstep_matches_dense(qs3g, precision):
         w = np.linalg.eigvalsh(om.build_sector(p["nod"], (p["K"], 0, 0)).dense())
         assert abs(r["ene"][0] - w[0]) <= 1e-9 * max(1.0, abs(w[0])), (r["ene"], w[:3])
         assert max(r["resid"]) <= 1e-10
+
+
+def test_trlan_lockstep_wide_basis_matches_dense(qs3g):
+    """NOM = 90: the device Ritz solves keep their NOM x NOM matrices in
+    global scratch instead of shared memory; same answers as dense."""
+    from ed_gb300 import sweep
+    probs = sweep.random_chains(seed=8, n=5, L_range=(24, 28), nods=(4,))
+    recs, _, _ = sweep.solve(probs, NOE=2, NOK=40, NOM=90, tol=1e-10, precision=1, lockstep=True)
+    for p, r in zip(probs, recs):
+        assert r["status"] == 0, r
+        b, jxy, jz = inputs.chain_bonds(p["L"], (1.0, p["delta"]), (p["j2"], p["j2"]))
+        om = O.Model(p["L"], p["L"], 1, 1, b, jxy, jz, kmax=p["nod"] + 2)
+        w = np.linalg.eigvalsh(om.build_sector(p["nod"], (p["K"], 0, 0)).dense())
+        assert abs(r["ene"][0] - w[0]) <= 1e-9 * max(1.0, abs(w[0])), (r["ene"], w[:3])
+        assert abs(r["ene"][1] - w[1]) <= 1e-9 * max(1.0, abs(w[1])), (r["ene"], w[:3])
+        assert max(r["resid"]) <= 1e-10
