@@ -301,7 +301,7 @@ def hv_variants(h, x, D, stream, dev, reps=10):
     forms = [("real_f64", lambda a, b: h.hv_real_device(a, b), xr, 8),
              ("complex_f32", lambda a, b: h.hv32_device(a, b), x32, 8),
              ("real_f32", lambda a, b: h.hv32_real_device(a, b), xr32, 4)]
-    for name, fn, xv, s in forms:
+    def timed(fn, xv):
         yv = torch.empty_like(xv)
         for _ in range(3):
             fn(xv.data_ptr(), yv.data_ptr())
@@ -312,10 +312,31 @@ def hv_variants(h, x, D, stream, dev, reps=10):
             fn(xv.data_ptr(), yv.data_ptr())
         ev1.record(stream)
         torch.cuda.synchronize(dev)
-        ms = ev0.elapsed_time(ev1) / reps
+        return ev0.elapsed_time(ev1) / reps, yv
+
+    for name, fn, xv, s in forms:
+        ms, yv = timed(fn, xv)
         B = D * (2 * s + 16) + nnz * (s + 8)
         out[name] = {"ms": ms, "algorithmic_gbs": B / (ms * 1e-3) / 1e9}
         del yv
+    # the same products from the cached connection table (qs3g_hv_cache):
+    # stream_gbs counts what the table form streams from HBM (table, x, y,
+    # diagonal, configuration: nb + D * (2 s + 16)); gathers of x(id) hit L2
+    _, y_mf = timed(lambda a, b: h.hv_device(a, b), x)
+    t0 = time.perf_counter()
+    nb = h.hv_cache(True)
+    torch.cuda.synchronize(dev)
+    tb = time.perf_counter() - t0
+    out["table"] = {"bytes": nb, "build_s": tb}
+    for name, fn, xv, s in [("complex_f64", lambda a, b: h.hv_device(a, b), x, 16)] + forms:
+        ms, yv = timed(fn, xv)
+        B = D * (2 * s + 16) + nnz * (s + 8)
+        out["table_" + name] = {"ms": ms, "algorithmic_gbs": B / (ms * 1e-3) / 1e9,
+                                "stream_gbs": (nb + D * (2 * s + 16)) / (ms * 1e-3) / 1e9}
+        if name == "complex_f64":
+            out["table_complex_f64"]["bit_identical_to_matrix_free"] = bool(torch.equal(yv, y_mf))
+        del yv
+    h.hv_cache(False)
     return out
 
 

@@ -37,7 +37,7 @@ EXPORTS = [
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
     "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real", "qs3g_set_time_limit", "qs3g_trlan_stats",
     "qs3g_build_sector_i32", "qs3g_get_sector_i32", "qs3g_load_sector", "qs3g_load_sector_i32",
-    "qs3g_hv32_real",
+    "qs3g_hv32_real", "qs3g_hv_cache",
 ]
 
 MLP_NPARAMS = 35329
@@ -291,6 +291,12 @@ class Handle:
         else:
             _check(rc, self.h)
         return dict(ene=ene, psi=psi, iters=int(iters.value), resid=resid, converged=(rc == OK))
+
+    def hv_cache(self, on=True):
+        """Cache (or drop) the sector's connection table on the device; returns its bytes."""
+        nb = C.c_int64(0)
+        _check(load().qs3g_hv_cache(self.h, _i(1 if on else 0), C.byref(nb)), self.h)
+        return int(nb.value)
 
     def set_time_limit(self, seconds):
         """Wall-clock limit of later trlan calls on this handle (0 = none)."""

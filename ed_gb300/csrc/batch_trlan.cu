@@ -15,6 +15,7 @@
 // arithmetic is double-float on the FP32 pipe (eft.cuh) for both storage
 // types, so complex(4) phases keep FP64-accurate reductions.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -61,13 +62,14 @@ __device__ __forceinline__ bool brow(const BSeg* segs, const int* bs, const int*
   return i < segs[sg].D;
 }
 
-// One block per active problem: fixed-order sum of its blocks' partials.
+// One block per active problem: fixed-order sum of its blocks' partials
+// (per of them for each block).
 // mode 0: out[s*ld] = sum; mode 1: out[s*ld] = (sqrt(sum.x), sum.x)
 __global__ void __launch_bounds__(kB) k_bfinal(const double2* part, const int* seg_b0, const int* seg_nb,
-                                               const int* active, double2* out, int64_t ld, int mode) {
+                                               const int* active, double2* out, int64_t ld, int mode, int per) {
   __shared__ double2 sh[kB];
   const int sg = active[blockIdx.x];
-  const int b0 = seg_b0[sg], nb = seg_nb[sg];
+  const int b0 = seg_b0[sg] * per, nb = seg_nb[sg] * per;
   double2 v = make_double2(0.0, 0.0);
   for (int b = threadIdx.x; b < nb; b += kB) {
     v.x += part[b0 + b].x;
@@ -712,19 +714,23 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
   for (auto& s : segs) maxchunk += (s.D + (int64_t)kB * kChunkTiles - 1) / ((int64_t)kB * kChunkTiles);
   int64_t maxblk = 0;
   for (auto& s : segs) maxblk += (s.D + kB - 1) / kB;
-  DevBuf<double2> part((size_t)std::max<int64_t>(maxblk, (int64_t)(NOM + 1) * maxchunk) + 1);
+  DevBuf<double2> part((size_t)std::max<int64_t>(kSegPartials * maxblk, (int64_t)(NOM + 1) * maxchunk) + 1);
   std::vector<int> hv_run(n, 0);
   auto col = [&](int j) { return V + (int64_t)j * ldv; };
   const BSeg* sg = d_segs.get();
 
-  auto final_ = [&](double2* out, int mode) {
-    k_bfinal<<<mp.nact, kB, 0, st>>>(part.get(), mp.d_sb0.get(), mp.d_snb.get(), mp.d_act.get(), out, Ls, mode);
+  auto final_ = [&](double2* out, int mode, int per) {
+    k_bfinal<<<mp.nact, kB, 0, st>>>(part.get(), mp.d_sb0.get(), mp.d_snb.get(), mp.d_act.get(), out, Ls, mode,
+                                      per);
     check_launch("k_bfinal");
   };
-  // Row form per NOD group: a group whose chains are all uniform with the
-  // same number of bond distances can take the unrolled uniform row; the
-  // faster of the two on this batch's data is kept (QS3G_SEG_FORM=general or
-  // uniform pins the choice).
+  // Row form per NOD group: the general chain row, the same with its
+  // general-path hops deferred to the end of the row (short chains send many
+  // hops there, and a warp otherwise pays for every hop position at which any
+  // of its rows does), or -- when every chain of the group is uniform with the
+  // same number of bond distances -- the unrolled uniform row.  The fastest
+  // on this batch's own data is kept; QS3G_SEG_FORM = general, deferred or
+  // uniform pins the choice.
   std::vector<int> seg_uni(9, 0);
   auto hv_group = [&](int g, int uni, const T* x, T* y, double2* pp) {
     if constexpr (sizeof(T) == sizeof(float2))
@@ -741,30 +747,43 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
     QS3G_CHECK_CUDA(cudaEventCreate(&e0));
     QS3G_CHECK_CUDA(cudaEventCreate(&e1));
     for (int g = 1; g <= 8; ++g) {
-      if (mp.gnblk[g] == 0 || form == "general") continue;
+      if (mp.gnblk[g] == 0) continue;
       int uno = -1;
       for (int s : mp.active)
         if (nod_of[s] == g) uno = (uno == -1 || uno == hs[s].uno) ? hs[s].uno : 0;
-      if (uno <= 0 || !seg_uniform_ok(g, uno)) continue;
-      if (form == "uniform") {
-        seg_uni[g] = uno;
-        continue;
+      bool tab = true;
+      for (int s : mp.active)
+        if (nod_of[s] == g) tab = tab && hs[s].tab != nullptr;
+      std::vector<int> cand{0, 3};
+      if (uno > 0 && seg_uniform_ok(g, uno)) cand.push_back(uno);
+      if (tab) cand.push_back(kSegTable);
+      if (form == "general") cand = {0};
+      else if (form == "deferred") cand = {3};
+      else if (form == "uniform") cand = {(uno > 0 && seg_uniform_ok(g, uno)) ? uno : 0};
+      else if (form == "table") cand = {tab ? kSegTable : 0};
+      std::vector<float> best(cand.size(), 1e30f);
+      if (cand.size() > 1)
+        for (int rep = 0; rep < 3; ++rep)
+          for (size_t f = 0; f < cand.size(); ++f) {
+            QS3G_CHECK_CUDA(cudaEventRecord(e0, st));
+            hv_group(g, cand[f], col(0), Q, part.get());
+            QS3G_CHECK_CUDA(cudaEventRecord(e1, st));
+            QS3G_CHECK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            QS3G_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep > 0) best[f] = std::min(best[f], ms);  // rep 0 warms up
+          }
+      const size_t k = (size_t)(std::min_element(best.begin(), best.end()) - best.begin());
+      seg_uni[g] = cand[k];
+      if (verbose()) {
+        std::printf("batched trlan: NOD %d group:", g);
+        for (size_t f = 0; f < cand.size(); ++f)
+          std::printf(" %s %.3f ms",
+                      cand[f] == 0 ? "general"
+                                   : (cand[f] == 3 ? "deferred" : (cand[f] == kSegTable ? "table" : "uniform")),
+                      best[f]);
+        std::printf("\n");
       }
-      float best[2] = {1e30f, 1e30f};
-      for (int rep = 0; rep < 3; ++rep)
-        for (int f = 0; f < 2; ++f) {
-          QS3G_CHECK_CUDA(cudaEventRecord(e0, st));
-          hv_group(g, f ? uno : 0, col(0), Q, part.get());
-          QS3G_CHECK_CUDA(cudaEventRecord(e1, st));
-          QS3G_CHECK_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          QS3G_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          if (rep > 0) best[f] = std::min(best[f], ms);  // rep 0 warms up
-        }
-      seg_uni[g] = best[1] < best[0] ? uno : 0;
-      if (verbose())
-        std::printf("batched trlan: NOD %d group, general %.3f ms, uniform %.3f ms -> %s\n", g, best[0], best[1],
-                    seg_uni[g] ? "uniform" : "general");
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -774,12 +793,12 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
   auto hvdot = [&](const T* x, T* y, double2* out) {
     for (int g = 1; g <= 8; ++g)
       if (mp.gnblk[g]) hv_group(g, seg_uni[g], x, y, part.get());
-    final_(out, 0);
+    final_(out, 0, kSegPartials);
   };
   auto nrm = [&](const T* x, double2* out) {
     k_bnrm<T><<<mp.nblk, kB, 0, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), x, part.get());
     check_launch("k_bnrm");
-    final_(out, 1);
+    final_(out, 1, 1);
   };
   auto scale = [&](T* x, const double2* s) {
     k_bscale<T><<<mp.nblk, kB, 0, st>>>(sg, mp.d_bs.get(), mp.d_bf.get(), x, s, Ls);
@@ -809,7 +828,7 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
                                                                          (int)Ls);
     check_launch("k_bgemv_final");
     gsub(ncols, ov.get(), col(i), part.get());
-    final_(beta.get() + i, 1);
+    final_(beta.get() + i, 1, 1);
   };
   const size_t rsm = ((size_t)NOM * NOK + (size_t)NOM * 32) * sizeof(float4);
   QS3G_CHECK_CUDA(cudaFuncSetAttribute(k_brestart<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
@@ -874,6 +893,7 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
     QS3G_CHECK_CUDA(e);
   };
 
+  const auto t_start = std::chrono::steady_clock::now();
   // ---- initial Lanczos pass
   nrm(col(0), beta.get());
   for (int i = 1; i <= NOM; ++i) {
@@ -891,7 +911,10 @@ void lockstep_core(const std::vector<BSeg>& segs, const std::vector<HvSeg>& hs, 
       if (mp.nact == 0) break;
       graph.reset();
     }
-    if (verbose()) std::printf("batched trlan: cycle %d, %d of %d problems active\n", cycle + 1, mp.nact, n);
+    if (verbose())
+      std::printf("batched trlan: cycle %d, %d of %d problems active (%lld rows), %.3f s\n", cycle + 1, mp.nact, n,
+                  (long long)mp.nblk * kB,
+                  std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count());
     if (can_capture && !graph.exec) capture();
     if (graph.exec) QS3G_CHECK_CUDA(cudaGraphLaunch(graph.exec, st));
     else restart_cycle();
@@ -948,6 +971,23 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
   DevBuf<double2> V64((size_t)ldv * (NOM + 1)), Q64(ldv);
   QS3G_CHECK_CUDA(cudaMemsetAsync(V64.get(), 0, (size_t)ldv * (NOM + 1) * sizeof(double2), st));
   QS3G_CHECK_CUDA(cudaMemsetAsync(Q64.get(), 0, ldv * sizeof(double2), st));
+  // Connection tables for the products: the sectors' own cached ones, else
+  // temporary ones while the device has room for them next to the Krylov
+  // vectors (the row form itself is chosen per NOD group by timing)
+  std::vector<HvTable> tmp_tab(n);
+  {
+    const char* env = std::getenv("QS3G_SEG_FORM");
+    const std::string form = env ? env : "auto";
+    if (form == "auto" || form == "table") {
+      const size_t keep = (p.precision == 1 ? (size_t)ldv * (NOM + 2) * sizeof(float2) : 0) + ((size_t)2 << 30);
+      for (int s = 0; s < n; ++s) {
+        if (secs[s]->tab.built() || hv_table_bytes(*models[s], *secs[s]) == 0) continue;
+        if (!build_hv_table(*models[s], *secs[s], tmp_tab[s], keep, st)) break;
+        set_seg_table(hs[s], tmp_tab[s]);
+      }
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(d_hs.get(), hs.data(), n * sizeof(HvSeg), cudaMemcpyHostToDevice, st));
+    }
+  }
   Maps all;
   all.nod_of = nod_of;
   all.build(segs, on, st);
@@ -1008,7 +1048,8 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
       k_bnrm<double2><<<mp.nblk, kB, 0, st>>>(d_segs.get(), mp.d_bs.get(), mp.d_bf.get(), W.get(), part.get());
       check_launch("k_bnrm");
       DevBuf<double2> rr(std::max(1, n));
-      k_bfinal<<<mp.nact, kB, 0, st>>>(part.get(), mp.d_sb0.get(), mp.d_snb.get(), mp.d_act.get(), rr.get(), 1, 1);
+      k_bfinal<<<mp.nact, kB, 0, st>>>(part.get(), mp.d_sb0.get(), mp.d_snb.get(), mp.d_act.get(), rr.get(), 1, 1,
+                                        1);
       check_launch("k_bfinal");
       std::vector<double2> hr(n);
       QS3G_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rr.get(), n * sizeof(double2), cudaMemcpyDeviceToHost, st));
@@ -1031,6 +1072,7 @@ int trlan_lockstep(const std::vector<const Model*>& models, const std::vector<co
       else again = true;
     }
     if (verbose()) std::printf("batched trlan: attempt %d, worst recomputed residual %.3e\n", attempt, worst);
+    if (verbose()) std::fflush(stdout);
     if (!again) break;
     tol_est *= 0.1;
     // continue the failing problems from the sum of their Ritz vectors

@@ -361,6 +361,24 @@ int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where)
   });
 }
 
+int qs3g_hv_cache(qs3g_handle h, const int* on, int64_t* bytes) {
+  return guarded(h, [&]() {
+    QS3G_REQUIRE(h && h->sector, QS3G_ESTATE, "no sector: call qs3g_build_sector first");
+    Sector& s = *h->sector;
+    QS3G_REQUIRE(on && (*on == 0 || *on == 1), QS3G_EINVAL, "on must be 0 or 1");
+    if (*on == 0) {
+      s.tab.release();
+    } else if (!s.tab.built()) {
+      QS3G_REQUIRE(hv_table_bytes(h->model, s) > 0, QS3G_ENOTSUP,
+                   "connection table: chain (NOD, K) sectors with indexable sizes only");
+      QS3G_REQUIRE(build_hv_table(h->model, s, s.tab, (size_t)1 << 30, h->stream), QS3G_ENOMEM,
+                   "connection table does not fit in device memory");
+    }
+    if (bytes) *bytes = (int64_t)s.tab.bytes();
+    return QS3G_OK;
+  });
+}
+
 int qs3g_hv_schedule(qs3g_handle h, const int* mode, int* chosen) {
   return guarded(h, [&]() {
     const Sector& s = need_sector(h);

@@ -69,6 +69,7 @@ struct HvArgs {
 };
 
 constexpr int kHvThreads = 256;
+static_assert(kSegPartials == kHvThreads / 32, "one alpha partial per warp of a batched product block");
 constexpr int kUniBlocks = 5;  // uniform chain rows: 40 resident warps per SM (<= 51 registers)
 
 // ------------------------------------------------------------ chain kernels
@@ -153,6 +154,16 @@ __device__ __forceinline__ int chain_hop_general(const HvArgs& a, const int (&n)
   return dir_lookup32(a.dir, anchored_index32<NOD>(p, a.binomA, a.L));
 }
 
+// The general hop out of line: the uniform rows unroll all their hops, and an
+// inlined copy of the general path per hop would crowd the instruction cache.
+// The row's configuration comes packed, so the caller's registers stay registers.
+template <int NOD>
+__device__ __noinline__ int chain_hop_slow(const HvArgs& a, uint64_t conf, int m, int e, int& ell, int& cnt) {
+  int n[NOD];
+  unpack<NOD>(conf, a.bits, n);
+  return chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+}
+
 // Chain rows work on the cyclic gaps g[k] = n[k+1] - n[k] (lane k; lane NOD-1
 // wraps).  A hop moves spin m by del = e - n[m] (taken the short way round the
 // ring); when it neither lands on nor passes another spin (|del| below the gap
@@ -166,7 +177,7 @@ __device__ __forceinline__ int chain_hop_general(const HvArgs& a, const int (&n)
 // the same (id, ell, count) as the general path, so the products are
 // bit-identical.  Moves onto or past another spin, tied largest gaps and a
 // single down spin take the general path.
-template <int NOD, bool KZERO, class V>
+template <int NOD, bool KZERO, class V, bool DEFER = false>
 __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restrict__ x, V* __restrict__ y,
                                              const double* __restrict__ diag,
                                              const typename Cplx<V>::R* __restrict__ coefR,
@@ -183,6 +194,7 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   const R di = (R)(__ldg(diag + i) - shift);  // shift applied in FP64 before rounding
   const int L = a.L, half = a.L >> 1;
   R ax = 0, ay = 0;
+  uint32_t pend = 0;  // DEFER: general-path hops (spin m, adjacency slot k) as bit 4 m + k
 #pragma unroll
   for (int m = 0; m < NOD; ++m) {
     const int d = n[m];
@@ -260,8 +272,36 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
 #pragma unroll
         for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
         if (edown) continue;  // parallel bond: diagonal only
+        if constexpr (DEFER) {
+          if (NOD <= 8 && t - e0 < 4) {
+            pend |= 1u << (4 * m + (t - e0));
+            continue;
+          }
+        }
         id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
       }
+      if (id < 0) continue;
+      V xv = x[id];
+      if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+      hop_acc(__ldg(coefR + (w >> 16) * (NOD + 1) + cnt), xv, ax, ay);
+    }
+  }
+  if constexpr (DEFER) {
+    // Deferred general-path hops: a warp runs this loop as often as its
+    // busiest lane has such hops, instead of once for every hop position
+    // at which any of its 32 rows needs the general path.
+    const uint64_t cw = __ldg(a.conf + i);
+    while (pend) {
+      const int slot = __ffs(pend) - 1;
+      pend &= pend - 1;
+      const int m = slot >> 2;
+      int d = n[0];
+#pragma unroll
+      for (int k = 1; k < NOD; ++k) d = (m == k) ? n[k] : d;
+      const uint32_t w = __ldg(a.adj + __ldg(a.adj_off + d) + (slot & 3));
+      const int e = (int)(w & 0xffffu);
+      int ell = 0, cnt = 1;
+      const int id = chain_hop_slow<NOD>(a, cw, m, e, ell, cnt);
       if (id < 0) continue;
       V xv = x[id];
       if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
@@ -272,15 +312,6 @@ __device__ __forceinline__ void hv_chain_row(const HvArgs& a, const V* __restric
   y[i] = row_out(di, xi, ir, ax, ay);
 }
 
-// The general hop out of line: the uniform rows unroll all their hops, and an
-// inlined copy of the general path per hop would crowd the instruction cache.
-// The row's configuration comes packed, so the caller's registers stay registers.
-template <int NOD>
-__device__ __noinline__ int chain_hop_slow(const HvArgs& a, uint64_t conf, int m, int e, int& ell, int& cnt) {
-  int n[NOD];
-  unpack<NOD>(conf, a.bits, n);
-  return chain_hop_general<NOD>(a, n, m, e, ell, cnt);
-}
 
 // Uniform chains: every site s carries a bond to s + o (mod L) for each of NO
 // distances o < L/2, with one coupling per distance (the chains of the XXZ
@@ -479,6 +510,155 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain32r(HvArgs a, const floa
 // ------------------------------------------------------------ batches of chain sectors
 // Block b works on segment blk_seg[b], rows (b - blk_first[b]) * 256 + tid of
 // it; the segment's tables replace the handle's in the row function.
+// ------------------------------------------------------------ cached connection table
+// The same products from the table that k_tab_build writes once per sector
+// (HvTable): per row the slots in the order the matrix-free row visits its
+// hops, each the target row and its coefficient, so the integer work of the
+// representative search is done once instead of at every product.  The FP64
+// sums take the same terms in the same order as hv_chain_row's, so the
+// complex(8) and real FP64 products equal the matrix-free ones bit for bit.
+struct TabArgs {
+  int64_t D;
+  int L, bits, slots;
+  const uint64_t* conf;
+  const uint32_t* tab;
+  const uint32_t* tabc;
+  const double* diag;
+  const double* coefR;
+  const float* coefR32;
+  const double* invR;
+  const float* invR32;
+  const double* tcoef;
+  const float* tcoef32;
+  const double2* chainph;
+  const float2* chainph32;
+};
+
+template <int NOD, bool PACKED, bool KZERO, class V, int SLOTS>
+__device__ __forceinline__ V tab_row(const TabArgs& t, const V* __restrict__ x, int64_t i, double shift) {
+  using R = typename Cplx<V>::R;
+  constexpr bool F64 = sizeof(R) == sizeof(double);
+  const R* coefR = [&] { if constexpr (F64) return t.coefR; else return t.coefR32; }();
+  const R* tcoef = [&] { if constexpr (F64) return t.tcoef; else return t.tcoef32; }();
+  const R* invR = [&] { if constexpr (F64) return t.invR; else return t.invR32; }();
+  const auto* ph = [&] { if constexpr (F64) return t.chainph; else return t.chainph32; }();
+  int n[NOD];
+  unpack<NOD>(__ldg(t.conf + i), t.bits, n);
+  const V xi = x[i];
+  const R di = (R)(__ldg(t.diag + i) - shift);
+  R ax = 0, ay = 0;
+  const int ns = SLOTS > 0 ? SLOTS : t.slots;
+#pragma unroll
+  for (int sl = 0; sl < (SLOTS > 0 ? SLOTS : 64); ++sl) {
+    if (SLOTS == 0 && sl >= ns) break;
+    const uint32_t e = __ldg(t.tab + (size_t)sl * t.D + i);
+    int id, ell = 0;
+    R c;
+    if constexpr (PACKED) {
+      if (e == 0xffffffffu) continue;
+      id = (int)(e & 0x7ffffffu);
+      c = __ldg(tcoef + (e >> 27));
+    } else {
+      id = (int)e;
+      if (id < 0) continue;
+      const uint32_t k = __ldg(t.tabc + (size_t)sl * t.D + i);
+      c = __ldg(coefR + (k & 0xffffu));
+      ell = (int)(k >> 16);
+    }
+    V xv = x[id];
+    if constexpr (!KZERO) xv = Cplx<V>::mul(__ldg(ph + ell), xv);
+    hop_acc(c, xv, ax, ay);
+  }
+  const R ir = __ldg(invR + chain_self_count<NOD>(n, t.L, t.bits));
+  return row_out(di, xi, ir, ax, ay);
+}
+
+template <int NOD, bool PACKED, bool KZERO, class V, int SLOTS>
+__global__ void __launch_bounds__(kHvThreads) k_hv_tab(TabArgs t, const V* __restrict__ x, V* __restrict__ y,
+                                                       double shift, int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < t.D) y[i] = tab_row<NOD, PACKED, KZERO, V, SLOTS>(t, x, i, shift);
+  else if (i == t.D && pad) y[i] = V{};
+}
+
+// One thread per row: the table entries of every slot of the row, from the
+// general hop (the fast paths of hv_chain_row give the same id, ell and
+// count).  bcls: distance index of each bond (packed form only).
+template <int NOD>
+__global__ void k_tab_build(HvArgs a, int deg, int packed, const uint8_t* __restrict__ bcls, uint32_t* tab,
+                            uint32_t* tabc) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.D) return;
+  int n[NOD];
+  unpack<NOD>(__ldg(a.conf + i), a.bits, n);
+  for (int m = 0; m < NOD; ++m) {
+    const int d = n[m];
+    const int e0 = __ldg(a.adj_off + d), e1 = __ldg(a.adj_off + d + 1);
+    for (int k = 0; k < deg; ++k) {
+      const size_t at = (size_t)(m * deg + k) * a.D + i;
+      uint32_t ent = 0xffffffffu, code = 0;
+      const int t = e0 + k;
+      if (t < e1) {
+        const uint32_t w = __ldg(a.adj + t);
+        const int e = (int)(w & 0xffffu);
+        bool edown = false;
+        for (int j = 0; j < NOD; ++j) edown |= (n[j] == e);
+        if (!edown) {
+          int ell = 0, cnt = 1;
+          const int id = chain_hop_general<NOD>(a, n, m, e, ell, cnt);
+          if (id >= 0) {
+            const uint32_t b = w >> 16;
+            if (packed) {
+              ent = (uint32_t)id | ((uint32_t)(bcls[b] * (NOD + 1) + cnt) << 27);
+            } else {
+              ent = (uint32_t)id;
+              code = ((uint32_t)ell << 16) | (b * (NOD + 1) + (uint32_t)cnt);
+            }
+          }
+        }
+      }
+      tab[at] = ent;
+      if (!packed) tabc[at] = code;
+    }
+  }
+}
+
+TabArgs tab_args(const Model& m, const Sector& s, const HvTable& t) {
+  TabArgs a{};
+  a.D = s.D; a.L = m.NOS; a.bits = m.bits; a.slots = t.slots;
+  a.conf = s.d_conf.get(); a.tab = t.tab.get(); a.tabc = t.tabc.get();
+  a.diag = s.d_diag.get(); a.coefR = s.d_coefR.get(); a.coefR32 = s.d_coefR32.get();
+  a.invR = s.d_invR.get(); a.invR32 = s.d_invR32.get();
+  a.tcoef = t.coef.get(); a.tcoef32 = t.coef32.get();
+  a.chainph = s.d_chainph.get(); a.chainph32 = s.d_chainph32.get();
+  return a;
+}
+
+// launch k_hv_tab for the sector's NOD, form and slot count (16 and 20 slots
+// -- NOD 4 and 5 with four bonds per site -- unrolled, others at run time)
+template <class V>
+void launch_tab(const Model& m, const Sector& s, const V* x, V* y, double shift, int pad, cudaStream_t st) {
+  const TabArgs a = tab_args(m, s, s.tab);
+  const unsigned grid = (unsigned)((s.D + pad + kHvThreads - 1) / kHvThreads);
+  auto go = [&](auto nod, auto pk, auto kz) {
+    constexpr int N = decltype(nod)::value;
+    constexpr bool P = decltype(pk)::value, Z = decltype(kz)::value;
+    if (a.slots == 4 * N && (N == 4 || N == 5))
+      k_hv_tab<N, P, Z, V, 4 * N><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pad);
+    else
+      k_hv_tab<N, P, Z, V, 0><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pad);
+  };
+  constexpr bool REAL = sizeof(V) == sizeof(typename Cplx<V>::R);
+  dispatch_nod(s.NOD, [&](auto c) {
+    using T = std::true_type;
+    using F = std::false_type;
+    if (s.tab.packed) go(c, T{}, T{});  // packed implies k = 0
+    else if (s.kzero) go(c, F{}, T{});
+    else if constexpr (!REAL) go(c, F{}, F{});  // real vectors only exist at k = 0
+  });
+  check_launch("k_hv_tab");
+}
+
 // Batched chain products, optionally with the Lanczos alpha partials in the
 // epilogue: when part is set, block b also writes sum over its rows of
 // conj(x_i) y_i (double-float, k_bdot's order) to part[seg_b0[s] + local
@@ -487,7 +667,6 @@ template <int NOD, int NO, class V>
 __device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const int* __restrict__ blk_seg,
                                         const int* __restrict__ blk_first, const V* __restrict__ x, V* __restrict__ y,
                                         double shift, double2* part, const int* __restrict__ seg_b0) {
-  __shared__ double2 sh[kHvThreads];
   const int sg = blk_seg[blockIdx.x];
   const HvSeg& g = segs[sg];
   const int lb = blockIdx.x - blk_first[blockIdx.x];
@@ -504,9 +683,18 @@ __device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const in
     const auto* cR = [&] { if constexpr (F64) return g.coefR; else return g.coefR32; }();
     const auto* iR = [&] { if constexpr (F64) return g.invR; else return g.invR32; }();
     const auto* ph = [&] { if constexpr (F64) return g.chainph; else return g.chainph32; }();
-    if constexpr (NO == 0) {
-      if (g.kzero) hv_chain_row<NOD, true, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
-      else hv_chain_row<NOD, false, V>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+    if constexpr (NO == 4) {
+      TabArgs t{};
+      t.D = g.D; t.L = g.L; t.bits = g.bits; t.slots = g.tslots;
+      t.conf = g.conf; t.tab = g.tab; t.tabc = g.tabc; t.diag = g.diag;
+      t.coefR = g.coefR; t.coefR32 = g.coefR32; t.invR = g.invR; t.invR32 = g.invR32;
+      t.tcoef = g.tcoef; t.tcoef32 = g.tcoef32; t.chainph = g.chainph; t.chainph32 = g.chainph32;
+      if (g.tpacked) ys[i] = tab_row<NOD, true, true, V, 0>(t, xs, i, sh_);
+      else if (g.kzero) ys[i] = tab_row<NOD, false, true, V, 0>(t, xs, i, sh_);
+      else ys[i] = tab_row<NOD, false, false, V, 0>(t, xs, i, sh_);
+    } else if constexpr (NO == 0 || NO == 3) {
+      if (g.kzero) hv_chain_row<NOD, true, V, NO == 3>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
+      else hv_chain_row<NOD, false, V, NO == 3>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
     } else {
       a.uno = NO;
 #pragma unroll
@@ -527,9 +715,18 @@ __device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const in
       df_fma(ih, il, fneg2(ui), vr);
     }
   }
-  if (part) {  // uniform across the block
-    const double2 t = block_sum2(make_double2(djoin(rh, rl), djoin(ih, il)), sh);
-    if (threadIdx.x == 0) part[seg_b0[sg] + lb] = t;
+  if (part) {  // one partial per warp, reduced in double-float: no barrier, no FP64
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float bh = __shfl_down_sync(0xffffffffu, rh, o), bl = __shfl_down_sync(0xffffffffu, rl, o);
+      const float ch = __shfl_down_sync(0xffffffffu, ih, o), cl = __shfl_down_sync(0xffffffffu, il, o);
+      df_add(rh, rl, bh);
+      rl = __fadd_rn(rl, bl);
+      df_add(ih, il, ch);
+      il = __fadd_rn(il, cl);
+    }
+    if ((threadIdx.x & 31) == 0)
+      part[(size_t)(seg_b0[sg] + lb) * kSegPartials + (threadIdx.x >> 5)] = make_double2(djoin(rh, rl), djoin(ih, il));
   }
 }
 
@@ -553,8 +750,10 @@ __global__ void __launch_bounds__(kHvThreads) k_hv_chain32_seg(const HvSeg* __re
   seg_row<NOD, NO, float2>(segs, blk_seg, blk_first, x, y, 0.0, part, seg_b0);
 }
 
-// (NOD, uniform distances) -> f(nod, no) with compile-time constants; no = 0
-// is the general row, uniform forms for NOD 2..6
+// (NOD, row form) -> f(nod, no) with compile-time constants: no = 0 the
+// general row, 1 or 2 the uniform row with that many bond distances (NOD
+// 2..6), 3 the general row with its general-path hops deferred, 4 the
+// connection table
 template <class F>
 void dispatch_seg(int NOD, int uni, F&& f) {
   if (uni >= 1 && uni <= 2 && NOD >= 2 && NOD <= 6) {
@@ -569,6 +768,13 @@ void dispatch_seg(int NOD, int uni, F&& f) {
       case 5: with_no(std::integral_constant<int, 5>{}); break;
       default: with_no(std::integral_constant<int, 6>{}); break;
     }
+    return;
+  }
+  if (uni == 3 || uni == kSegTable) {
+    dispatch_nod(NOD, [&](auto c) {
+      if (uni == 3) f(c, std::integral_constant<int, 3>{});
+      else f(c, std::integral_constant<int, kSegTable>{});
+    });
     return;
   }
   dispatch_nod(NOD, [&](auto c) { f(c, std::integral_constant<int, 0>{}); });
@@ -1031,7 +1237,17 @@ HvSeg make_seg(const Model& m, const Sector& s, int64_t row0) {
     g.uoff[k] = k < m.uni_no ? m.uni_off[k] : 0;
     g.ubond[k] = k < m.uni_no ? m.uni_bond[k] : 0;
   }
+  set_seg_table(g, s.tab);
   return g;
+}
+
+void set_seg_table(HvSeg& g, const HvTable& t) {
+  g.tab = t.built() ? t.tab.get() : nullptr;
+  g.tabc = t.built() ? t.tabc.get() : nullptr;
+  g.tcoef = t.coef.get();
+  g.tcoef32 = t.coef32.get();
+  g.tslots = t.slots;
+  g.tpacked = t.packed ? 1 : 0;
 }
 
 bool seg_uniform_ok(int NOD, int uni) { return uni >= 1 && uni <= 2 && NOD >= 2 && NOD <= 6; }
@@ -1081,8 +1297,77 @@ void compute_diag(const Model& m, Sector& s, cudaStream_t st) {
   check_launch("k_diag");
 }
 
+static bool table_layout(const Model& m, const Sector& s, int& deg, bool& packed) {
+  if (!s.anchored || s.u1 || s.D <= 0 || !m.chain) return false;
+  deg = 0;
+  for (int d = 1; d <= m.NOS; ++d) deg = std::max(deg, m.adj_off[d + 1] - m.adj_off[d]);
+  if (deg == 0 || s.NOD * deg > 64) return false;
+  packed = s.kzero && m.uni_no >= 1 && s.D < (int64_t(1) << 27) && m.uni_no * (s.NOD + 1) <= 31;
+  if (!packed && (s.D >= (int64_t(1) << 31) || (int64_t)m.NOxxz * (s.NOD + 1) >= 65536 || m.NOS >= 65536))
+    return false;
+  return true;
+}
+
+size_t hv_table_bytes(const Model& m, const Sector& s) {
+  int deg;
+  bool packed;
+  if (!table_layout(m, s, deg, packed)) return 0;
+  return (size_t)s.NOD * deg * (size_t)s.D * sizeof(uint32_t) * (packed ? 1 : 2);
+}
+
+bool build_hv_table(const Model& m, const Sector& s, HvTable& t, size_t keep, cudaStream_t st) {
+  t.release();
+  int deg;
+  bool packed;
+  QS3G_REQUIRE(table_layout(m, s, deg, packed), QS3G_ENOTSUP,
+               "connection table: chain (NOD, K) sectors with indexable sizes only");
+  const size_t bytes = hv_table_bytes(m, s);
+  size_t free_b = 0, total_b = 0;
+  QS3G_CHECK_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (bytes + keep > free_b) return false;
+  const size_t n = (size_t)s.NOD * deg * (size_t)s.D;
+  t.tab.alloc(n);
+  if (!packed) t.tabc.alloc(n);
+  DevBuf<uint8_t> bcls(std::max(1, m.NOxxz));
+  const int nc = s.NOD + 1;
+  t.coef.alloc(32);
+  t.coef32.alloc(32);
+  if (packed) {
+    std::vector<uint8_t> hb(m.NOxxz, 0);
+    for (int b = 0; b < m.NOxxz; ++b) {
+      const int o = m.p2[b] - m.p1[b];
+      const int dk = std::min(o, m.NOS - o);
+      hb[b] = (m.uni_no > 1 && dk == m.uni_off[1]) ? 1 : 0;
+    }
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(bcls.get(), hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
+    // class k * (NOD + 1) + c takes the coefficient of the distance's first bond (all equal)
+    for (int k = 0; k < m.uni_no; ++k) {
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(t.coef.get() + k * nc, s.d_coefR.get() + (size_t)m.uni_bond[k] * nc,
+                                      nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      QS3G_CHECK_CUDA(cudaMemcpyAsync(t.coef32.get() + k * nc, s.d_coefR32.get() + (size_t)m.uni_bond[k] * nc,
+                                      nc * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  const HvArgs a = make_args(m, s);
+  const unsigned grid = (unsigned)((s.D + 127) / 128);
+  dispatch_nod(s.NOD, [&](auto c) {
+    k_tab_build<decltype(c)::value><<<grid, 128, 0, st>>>(a, deg, packed ? 1 : 0, bcls.get(), t.tab.get(),
+                                                          t.tabc.get());
+  });
+  check_launch("k_tab_build");
+  QS3G_CHECK_CUDA(cudaStreamSynchronize(st));  // bcls goes out of scope
+  t.slots = s.NOD * deg;
+  t.deg = deg;
+  t.packed = packed;
+  return true;
+}
+
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
   if (s.D == 0) return;
+  if (s.tab.built()) {
+    launch_tab<double2>(m, s, x, y, 0.0, 0, st);
+    return;
+  }
   const HvArgs a = make_args(m, s);
   if (s.u1) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);
@@ -1111,6 +1396,10 @@ void hv64r(const Model& m, const Sector& s, const double* x, double* y, cudaStre
   if (s.D == 0) return;
   const HvArgs a = make_args(m, s);
   const int pr = (pad && (s.D & 1)) ? 1 : 0;
+  if (s.tab.built()) {
+    launch_tab<double>(m, s, x, y, 0.0, pr, st);
+    return;
+  }
   const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
   // the general chain row, as the complex(8) product uses: the real product
   // stays the real part of the complex one bit for bit
@@ -1126,6 +1415,10 @@ void hv32r(const Model& m, const Sector& s, const float* x, float* y, cudaStream
   if (s.D == 0) return;
   const HvArgs a = make_args(m, s);
   const int pr = (pad && (s.D & 1)) ? 1 : 0;
+  if (s.tab.built()) {
+    launch_tab<float>(m, s, x, y, (double)shift, pr, st);
+    return;
+  }
   const unsigned grid = (unsigned)((s.D + pr + kHvThreads - 1) / kHvThreads);
   const bool uni = !s.u1 && dispatch_uniform(m, s, [&](auto c, auto no) {
     k_hv_uchain32r<decltype(c)::value, decltype(no)::value><<<grid, kHvThreads, 0, st>>>(a, x, y, shift, pr);
@@ -1185,6 +1478,10 @@ void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y,
 
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift) {
   if (s.D == 0) return;
+  if (s.tab.built()) {
+    launch_tab<float2>(m, s, x, y, (double)shift, 0, st);
+    return;
+  }
   const HvArgs a = make_args(m, s);
   if (s.u1) {
     const unsigned grid = (unsigned)((s.D + kHvThreads - 1) / kHvThreads);

@@ -69,17 +69,26 @@ struct HvSeg {
   double shift;             // per-sector shift of the complex(4) product (H - shift)
   int uno;                  // uniform chain: number of bond distances (0: not uniform)
   int uoff[2], ubond[2];    //   the distances and one bond of each
+  const uint32_t* tab;      // connection table (HvTable), or null
+  const uint32_t* tabc;
+  const double* tcoef;
+  const float* tcoef32;
+  int tslots, tpacked;
 };
 
 HvSeg make_seg(const Model& m, const Sector& s, int64_t row0);
+// point a segment at a connection table (or at none, when t is not built)
+void set_seg_table(HvSeg& g, const HvTable& t);
 
 // H*v - shift*v over a batch of chain sectors with the same NOD: one launch,
 // block b serves segment blk_seg[b] (blocks of 256 rows, each segment padded
-// to whole blocks).  With part set, block b also stores its rows' share of
-// <x, y> at part[seg_b0[segment] + b - blk_first[b]].
+// to whole blocks).  With part set, warp w of block b also stores its rows'
+// share of <x, y> at part[8 * (seg_b0[segment] + b - blk_first[b]) + w].
 // uni = 1 or 2: every segment of the launch is a uniform chain with that many
 // bond distances, and the rows take hv_uchain_row's unrolled form (the same
-// hops summed in another order); uni = 0: the general chain row.
+// hops summed in another order); uni = 0: the general chain row; uni = 3:
+// the general row with its general-path hops summed after the others.
+constexpr int kSegPartials = 8;  // alpha partials per 256-row block (one per warp)
 void hv64_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_blk_first, int nblk,
               const double2* x, double2* y, double shift, cudaStream_t st, double2* part = nullptr,
               const int* seg_b0 = nullptr, int uni = 0);
@@ -89,6 +98,9 @@ void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_b
               int uni = 0);
 // true when the uniform form exists for NOD and uni
 bool seg_uniform_ok(int NOD, int uni);
+// uni = 4: every segment of the launch reads its connection table
+// (HvSeg::tab set, all packed or all wide)
+constexpr int kSegTable = 4;
 
 
 struct TrlanParams {

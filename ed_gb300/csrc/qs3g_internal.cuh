@@ -108,6 +108,29 @@ struct Model {
 
 // ---------------------------------------------------------------- sector
 // A (NOD, K) representative basis (allocate_lists_omp_SQ, state_lists.f90:225-292).
+// Cached connection table of a chain sector (qs3g_hv_cache): for every row
+// and hop slot (down spin m, adjacency slot k of its site: slot m * deg + k,
+// the order in which the matrix-free row visits its hops) the target row and
+// what its coefficient needs, stored slot-major (entry [slot * D + row]) so a
+// warp's loads of one slot are coalesced.  Packed form (k = 0 uniform chains,
+// D < 2^27): id | class << 27 with class = distance index * (NOD + 1) +
+// self-translation count, 0xffffffff for no hop; wide form: id (-1 for no
+// hop) plus a code plane ell << 16 | (bond * (NOD + 1) + count).
+struct HvTable {
+  DevBuf<uint32_t> tab, tabc;
+  DevBuf<double> coef;   // packed: coefficient per class
+  DevBuf<float> coef32;
+  int slots = 0, deg = 0;
+  bool packed = false;
+  bool built() const { return slots > 0; }
+  size_t bytes() const { return (tab.n + tabc.n) * sizeof(uint32_t); }
+  void release() {
+    tab.release(); tabc.release(); coef.release(); coef32.release();
+    slots = deg = 0;
+    packed = false;
+  }
+};
+
 struct Sector {
   int NOD = 0;
   int K[3] = {0, 0, 0};
@@ -136,6 +159,7 @@ struct Sector {
   // general-lattice H*v schedule per precision: 0 = pick on first use,
   // 1 = warp per row, 2 = thread per row (identical results)
   mutable int hv_schedule64 = 0, hv_schedule32 = 0;
+  HvTable tab;                      // built by qs3g_hv_cache; every chain H*v then reads it
 };
 
 // Host-side explist (input_param.f90:87-89) and checkstate phases
@@ -146,6 +170,12 @@ void host_explist(const double rk[3], int LX, int LY, int LZ, std::vector<double
 
 // ---------------------------------------------------------------- kernels (host wrappers)
 void build_sector(const Model& m, int NOD, const int K[3], Sector& s, cudaStream_t st);
+
+// Bytes the connection table of s would take (0: not a chain sector, or a
+// size the table formats cannot index), and its build: false when the device
+// lacks the memory (keep = free bytes to leave).
+size_t hv_table_bytes(const Model& m, const Sector& s);
+bool build_hv_table(const Model& m, const Sector& s, HvTable& t, size_t keep, cudaStream_t st);
 
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
 // complex(4) H*v of H - shift (shift = 0 for the plain product)

@@ -79,6 +79,14 @@ module qs3g_iface
       integer(c_int) :: where
     end function
 
+    ! cache (on = 1) or drop (on = 0) the sector's connection table
+    integer(c_int) function qs3g_hv_cache(h, on, bytes) bind(C, name="qs3g_hv_cache")
+      import :: c_ptr, c_int, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int) :: on
+      integer(c_int64_t) :: bytes
+    end function
+
     ! wall-clock limit of qs3g_trlan, and what the last qs3g_trlan did
     integer(c_int) function qs3g_set_time_limit(h, seconds) bind(C, name="qs3g_set_time_limit")
       import :: c_ptr, c_int, c_double

@@ -157,6 +157,23 @@ int qs3g_hv32_real(qs3g_handle h, float* v0, const float* v1, const float* shift
  * counterpart in the reference. */
 int qs3g_hv_schedule(qs3g_handle h, const int* mode, int* chosen);
 
+/* Cache the current chain sector's connection table in device memory (on =
+ * 1) or drop it (on = 0).  The table holds, per row and hop, the target row
+ * and its coefficient (4 bytes per hop for k = 0 chains with one coupling per
+ * bond distance, 8 otherwise: NOD * (bonds per site) hops per row, e.g.
+ * 2.65 GB for L = 1000, N_down = 4 with NN + NNN bonds); while it is cached,
+ * every H*v of the sector (qs3g_hv, qs3g_hv_real, qs3g_hv32_real, qs3g_trlan,
+ * qs3g_trlan_lockstep) reads it instead of searching representatives per
+ * hop.  complex(8) and real FP64 products are bit-identical with and
+ * without it; complex(4) and real FP32 ones may differ in rounding (the
+ * matrix-free FP32 form sums the hops in another order).  bytes (may be NULL)
+ * receives the table's size, 0 when none is cached.  QS3G_ENOTSUP for
+ * U(1) sectors and general lattices, QS3G_ENOMEM when it does not fit with
+ * 1 GiB to spare.  A new qs3g_build_sector drops it.  No counterpart in the
+ * reference (ham_to_vec_wave_vector, source/ham2vec_v3.f90:37-72, searches
+ * every hop at every product). */
+int qs3g_hv_cache(qs3g_handle h, const int* on, int64_t* bytes);
+
 /* The connection table of ham_to_vec_wave_vector: one entry per antiparallel
  * bond whose hop lands on a row of the sector (the `id > 0` branch of
  * source/ham2vec_v3.f90:61-65): 1-based row and column, the translation
