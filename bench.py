@@ -416,6 +416,8 @@ def solve_arm(args):
     D = h.build_sector(NOD, (0, 0, 0))
     if use_net:
         v = learned.start_vector(net, h, delta, j2)
+    if args.table:
+        h.hv_cache(True)
     h.set_time_limit(args.arm_limit)
     t0 = time.perf_counter()
     r = h.trlan(1, args.nok, args.nom, maxitr=args.maxrestart, tol=args.tol, precision=prec, conv_mode=1, seed=7,
@@ -461,6 +463,9 @@ def solve_bench(args):
     t0 = time.perf_counter()
     v = learned.start_vector(net, h, delta, j2)
     out["network"]["predict_s"] = time.perf_counter() - t0
+    if args.table:  # both arms read the cached connection table
+        t0 = time.perf_counter()
+        out["hv_table"] = {"bytes": h.hv_cache(True), "build_s": time.perf_counter() - t0}
     runs = [("learned_fp32_real", 1 | capi.REAL, v, 0.0)]
     if args.solve_all:
         runs += [("learned_fp32", 1, v, 0.0), ("random_fp32", 1, None, 0.0),
@@ -519,6 +524,8 @@ def cfg5_bench(args):
         h = learned.chain_handle(L, delta, j2)
         D = h.build_sector(NOD, (0, 0, 0))
         v = learned.start_vector(net, h, delta, j2)
+        if args.table:
+            h.hv_cache(True)
         rec = {"sector_dim": D}
         for name, start in (("learned", v), ("random", None)):
             h.set_time_limit(args.cfg5_limit)
@@ -542,23 +549,35 @@ def batch_bench(args):
     """The batched-solve workload: 256 XXZ chains from seed 1 (L in
     {48..128}, N_down in {3, 4, 5}, k over the L momenta, Delta in [0, 2],
     J2 in [0, 0.5]), lowest 2 eigenpairs each to ||r|| <= 1e-10 with FP32
-    Krylov vectors and FP64 reductions.  Both solvers from the same sectors:
-    qs3g_trlan_lockstep (all problems in one graph-replayed launch sequence)
-    and qs3g_trlan_batch (one stream per host thread, 8 threads)."""
+    Krylov vectors and FP64 reductions, from the same sectors:
+      lockstep                   qs3g_trlan_lockstep: all problems in one
+                                 graph-replayed launch sequence, row forms
+                                 autotuned (it builds connection tables itself);
+      batch_8_streams            qs3g_trlan_batch: each problem's own
+                                 qs3g_trlan on its own stream, 8 host threads,
+                                 matrix-free products;
+      batch_8_streams_tables     the same with every sector's connection table
+                                 cached first (qs3g_hv_cache)."""
     from ed_gb300 import sweep
     probs = sweep.random_chains(seed=1, n=args.batch_n)
     out = {"workload": f"{args.batch_n}_random_xxz_chains_L48-128_Ndown3-5_lowest2_tol1e-10_fp32_vectors",
            "NOE": 2, "NOK": 8, "NOM": 24}
-    for name, lock in (("lockstep", True), ("batch_8_streams", False)):
-        recs, tb, ts = sweep.solve(probs, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, lockstep=lock)
+    arms = [("lockstep", True, False), ("batch_8_streams", False, False)]
+    if args.table:
+        arms.append(("batch_8_streams_tables", False, True))
+    e0 = None
+    for name, lock, cache in arms:
+        recs, tb, ts = sweep.solve(probs, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, lockstep=lock,
+                                   hv_cache=cache)
         out[name] = {"solve_s": ts, "build_s": tb, "all_ok": all(r["status"] == 0 for r in recs),
                      "max_resid": max(max(r["resid"]) for r in recs), "hv_total": sum(r["hv"] for r in recs)}
         out.setdefault("rows_total", sum(r["D"] for r in recs))
-        out.setdefault("E0", [r["ene"][0] for r in recs])
-        if name == "batch_8_streams":
-            out["max_dE0_lockstep_vs_batch"] = max(abs(a - r["ene"][0]) for a, r in zip(out["E0"], recs))
-    out.pop("E0")
-    out["speedup_lockstep_vs_batch"] = out["batch_8_streams"]["solve_s"] / out["lockstep"]["solve_s"]
+        if e0 is None:
+            e0 = [r["ene"][0] for r in recs]
+        else:
+            out[name]["max_dE0_vs_lockstep"] = max(abs(a - r["ene"][0]) for a, r in zip(e0, recs))
+    for name, _, _ in arms[1:]:
+        out[f"speedup_lockstep_vs_{name}"] = out[name]["solve_s"] / out["lockstep"]["solve_s"]
     return out
 
 
@@ -616,6 +635,8 @@ def main():
     ap.add_argument("--batch", action="store_true",
                     help="add the batched solves (256 random chains): lock step against concurrent streams")
     ap.add_argument("--batch-n", type=int, default=256, help="problems in --batch")
+    ap.add_argument("--no-table", dest="table", action="store_false",
+                    help="solves without the cached connection table (matrix-free H*v only)")
     ap.add_argument("--cfg5", action="store_true",
                     help="add the learned-vs-random start comparison at (Delta, J2) = (0.7, 0.25), L = 200 and 400")
     ap.add_argument("--cfg5-limit", type=float, default=300.0, help="wall seconds per --cfg5 solve")

@@ -532,6 +532,8 @@ struct TabArgs {
   const float* tcoef32;
   const double2* chainph;
   const float2* chainph32;
+  const float2* coefS;
+  const float4* phS;
 };
 
 template <int NOD, bool PACKED, bool KZERO, class V, int SLOTS>
@@ -571,6 +573,90 @@ __device__ __forceinline__ V tab_row(const TabArgs& t, const V* __restrict__ x, 
   }
   const R ir = __ldg(invR + chain_self_count<NOD>(n, t.L, t.bits));
   return row_out(di, xi, ir, ax, ay);
+}
+
+// The complex(8) table row in double-float arithmetic on the FP32 pipe:
+// x(id) split with integer instructions (dsplit), phases and coefficients
+// from pre-split tables, sums as unevaluated float pairs; one FP64 subtraction
+// (diagonal - shift) and the final joins per row.  GB300 runs FP64 at 1/64 of
+// the FP32 rate, and a k != 0 hop costs 6 FP64 operations in FP64.
+template <int NOD, bool PACKED, bool KZERO, class V = double2>
+__device__ __forceinline__ V tab_row_df(const TabArgs& t, const V* __restrict__ x, int64_t i, double shift) {
+  constexpr bool CPLX = sizeof(V) == sizeof(double2);
+  int n[NOD];
+  unpack<NOD>(__ldg(t.conf + i), t.bits, n);
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  for (int sl = 0; sl < t.slots; ++sl) {
+    const uint32_t e = __ldg(t.tab + (size_t)sl * t.D + i);
+    int id, ell = 0;
+    float2 c;
+    if constexpr (PACKED) {
+      if (e == 0xffffffffu) continue;
+      id = (int)(e & 0x7ffffffu);
+      c = __ldg(t.coefS + (e >> 27));
+    } else {
+      id = (int)e;
+      if (id < 0) continue;
+      const uint32_t k = __ldg(t.tabc + (size_t)sl * t.D + i);
+      c = __ldg(t.coefS + (k & 0xffffu));
+      ell = (int)(k >> 16);
+    }
+    float2 xr, xm = make_float2(0.f, 0.f);
+    if constexpr (CPLX) {
+      const double2 xv = x[id];
+      xr = dsplit(xv.x);
+      xm = dsplit(xv.y);
+    } else {
+      xr = dsplit(x[id]);
+    }
+    if constexpr (!KZERO && CPLX) {
+      const float4 p = __ldg(t.phS + ell);
+      const float2 pr = make_float2(p.x, p.y), pm = make_float2(p.z, p.w);
+      float zrh = 0.f, zrl = 0.f, zmh = 0.f, zml = 0.f;
+      df_fma(zrh, zrl, pr, xr);
+      df_fma(zrh, zrl, fneg2(pm), xm);
+      df_fma(zmh, zml, pr, xm);
+      df_fma(zmh, zml, pm, xr);
+      xr = make_float2(zrh, zrl);
+      xm = make_float2(zmh, zml);
+    }
+    df_fma(rh, rl, c, xr);
+    if constexpr (CPLX) df_fma(ih, il, c, xm);
+  }
+  const float2 d = dsplit(__ldg(t.diag + i) - shift);
+  const float2 ir = dsplit(__ldg(t.invR + chain_self_count<NOD>(n, t.L, t.bits)));
+  float yrh = 0.f, yrl = 0.f, ymh = 0.f, yml = 0.f;
+  if constexpr (CPLX) {
+    const double2 xi = x[i];
+    df_fma(yrh, yrl, d, dsplit(xi.x));
+    df_fma(ymh, yml, d, dsplit(xi.y));
+    df_fma(yrh, yrl, ir, make_float2(rh, rl));
+    df_fma(ymh, yml, ir, make_float2(ih, il));
+    return make_double2(djoin(yrh, yrl), djoin(ymh, yml));
+  } else {
+    df_fma(yrh, yrl, d, dsplit(x[i]));
+    df_fma(yrh, yrl, ir, make_float2(rh, rl));
+    return djoin(yrh, yrl);
+  }
+}
+
+template <int NOD, bool PACKED, bool KZERO, class V>
+__global__ void __launch_bounds__(kHvThreads) k_hv_tab_df(TabArgs t, const V* __restrict__ x, V* __restrict__ y,
+                                                          int pad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < t.D) y[i] = tab_row_df<NOD, PACKED, KZERO, V>(t, x, i, 0.0);
+  else if (i == t.D && pad) y[i] = V{};
+}
+
+// split copies of a sector's phases and coefficients for tab_row_df
+__global__ void k_split_tables(const double2* __restrict__ ph, int nph, float4* phS, const double* __restrict__ cf,
+                               int ncf, float2* cfS) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nph) {
+    const float2 r = dsplit(ph[k].x), m = dsplit(ph[k].y);
+    phS[k] = make_float4(r.x, r.y, m.x, m.y);
+  }
+  if (k < ncf) cfS[k] = dsplit(cf[k]);
 }
 
 template <int NOD, bool PACKED, bool KZERO, class V, int SLOTS>
@@ -631,7 +717,23 @@ TabArgs tab_args(const Model& m, const Sector& s, const HvTable& t) {
   a.invR = s.d_invR.get(); a.invR32 = s.d_invR32.get();
   a.tcoef = t.coef.get(); a.tcoef32 = t.coef32.get();
   a.chainph = s.d_chainph.get(); a.chainph32 = s.d_chainph32.get();
+  a.coefS = t.coefS.get(); a.phS = t.phS.get();
   return a;
+}
+
+// the complex(8) / real FP64 table product in double-float arithmetic
+template <class V>
+void launch_tab_df(const Model& m, const Sector& s, const V* x, V* y, int pad, cudaStream_t st) {
+  const TabArgs a = tab_args(m, s, s.tab);
+  const unsigned grid = (unsigned)((s.D + pad + kHvThreads - 1) / kHvThreads);
+  constexpr bool REAL = sizeof(V) == sizeof(double);
+  dispatch_nod(s.NOD, [&](auto c) {
+    constexpr int N = decltype(c)::value;
+    if (s.tab.packed) k_hv_tab_df<N, true, true, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    else if (s.kzero) k_hv_tab_df<N, false, true, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    else if constexpr (!REAL) k_hv_tab_df<N, false, false, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+  });
+  check_launch("k_hv_tab_df");
 }
 
 // launch k_hv_tab for the sector's NOD, form and slot count (16 and 20 slots
@@ -689,9 +791,16 @@ __device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const in
       t.conf = g.conf; t.tab = g.tab; t.tabc = g.tabc; t.diag = g.diag;
       t.coefR = g.coefR; t.coefR32 = g.coefR32; t.invR = g.invR; t.invR32 = g.invR32;
       t.tcoef = g.tcoef; t.tcoef32 = g.tcoef32; t.chainph = g.chainph; t.chainph32 = g.chainph32;
-      if (g.tpacked) ys[i] = tab_row<NOD, true, true, V, 0>(t, xs, i, sh_);
-      else if (g.kzero) ys[i] = tab_row<NOD, false, true, V, 0>(t, xs, i, sh_);
-      else ys[i] = tab_row<NOD, false, false, V, 0>(t, xs, i, sh_);
+      t.coefS = g.tcoefS; t.phS = g.tphS;
+      if constexpr (F64) {
+        if (g.tpacked) ys[i] = tab_row_df<NOD, true, true>(t, xs, i, sh_);
+        else if (g.kzero) ys[i] = tab_row_df<NOD, false, true>(t, xs, i, sh_);
+        else ys[i] = tab_row_df<NOD, false, false>(t, xs, i, sh_);
+      } else {
+        if (g.tpacked) ys[i] = tab_row<NOD, true, true, V, 0>(t, xs, i, sh_);
+        else if (g.kzero) ys[i] = tab_row<NOD, false, true, V, 0>(t, xs, i, sh_);
+        else ys[i] = tab_row<NOD, false, false, V, 0>(t, xs, i, sh_);
+      }
     } else if constexpr (NO == 0 || NO == 3) {
       if (g.kzero) hv_chain_row<NOD, true, V, NO == 3>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
       else hv_chain_row<NOD, false, V, NO == 3>(a, xs, ys, g.diag, cR, iR, ph, i, sh_);
@@ -1246,6 +1355,8 @@ void set_seg_table(HvSeg& g, const HvTable& t) {
   g.tabc = t.built() ? t.tabc.get() : nullptr;
   g.tcoef = t.coef.get();
   g.tcoef32 = t.coef32.get();
+  g.tcoefS = t.coefS.get();
+  g.tphS = t.phS.get();
   g.tslots = t.slots;
   g.tpacked = t.packed ? 1 : 0;
 }
@@ -1332,6 +1443,8 @@ bool build_hv_table(const Model& m, const Sector& s, HvTable& t, size_t keep, cu
   const int nc = s.NOD + 1;
   t.coef.alloc(32);
   t.coef32.alloc(32);
+  QS3G_CHECK_CUDA(cudaMemsetAsync(t.coef.get(), 0, 32 * sizeof(double), st));
+  QS3G_CHECK_CUDA(cudaMemsetAsync(t.coef32.get(), 0, 32 * sizeof(float), st));
   if (packed) {
     std::vector<uint8_t> hb(m.NOxxz, 0);
     for (int b = 0; b < m.NOxxz; ++b) {
@@ -1355,6 +1468,13 @@ bool build_hv_table(const Model& m, const Sector& s, HvTable& t, size_t keep, cu
                                                           t.tabc.get());
   });
   check_launch("k_tab_build");
+  const int nph = (int)s.d_chainph.n;
+  const int ncf = packed ? 32 : (int)s.d_coefR.n;
+  t.phS.alloc(std::max(1, nph));
+  t.coefS.alloc(std::max(1, ncf));
+  k_split_tables<<<(unsigned)((std::max(nph, ncf) + 255) / 256), 256, 0, st>>>(
+      s.d_chainph.get(), nph, t.phS.get(), packed ? t.coef.get() : s.d_coefR.get(), ncf, t.coefS.get());
+  check_launch("k_split_tables");
   QS3G_CHECK_CUDA(cudaStreamSynchronize(st));  // bcls goes out of scope
   t.slots = s.NOD * deg;
   t.deg = deg;
@@ -1386,6 +1506,18 @@ void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStr
   } else {
     hv64_general(m, s, x, y, st);
   }
+}
+
+bool hv64_df(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st) {
+  if (!s.tab.built() || s.D == 0) return false;
+  launch_tab_df<double2>(m, s, x, y, 0, st);
+  return true;
+}
+
+bool hv64r_df(const Model& m, const Sector& s, const double* x, double* y, cudaStream_t st, bool pad) {
+  if (!s.tab.built() || s.D == 0 || !s.kzero) return false;
+  launch_tab_df<double>(m, s, x, y, (pad && (s.D & 1)) ? 1 : 0, st);
+  return true;
 }
 
 bool real_sector(const Sector& s) { return s.u1 || (s.anchored && s.kzero); }

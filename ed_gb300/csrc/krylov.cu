@@ -950,16 +950,23 @@ template <class T>
 struct HvOp;
 template <>
 struct HvOp<double2> {
+  // eft: the double-float modes, which read a cached connection table in
+  // double-float arithmetic too (FP64 arithmetic otherwise)
   static void apply(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st, double,
-                    bool real) {
-    if (real) hv64r(m, s, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), st, true);
-    else hv64(m, s, x, y, st);
+                    bool real, bool eft = false) {
+    if (real) {
+      auto* xr = reinterpret_cast<const double*>(x);
+      auto* yr = reinterpret_cast<double*>(y);
+      if (!(eft && hv64r_df(m, s, xr, yr, st, true))) hv64r(m, s, xr, yr, st, true);
+    } else if (!(eft && hv64_df(m, s, x, y, st))) {
+      hv64(m, s, x, y, st);
+    }
   }
 };
 template <>
 struct HvOp<float2> {
   static void apply(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, double shift,
-                    bool real) {
+                    bool real, bool = false) {
     if (real) hv32r(m, s, reinterpret_cast<const float*>(x), reinterpret_cast<float*>(y), st, (float)shift, true);
     else hv32(m, s, x, y, st, (float)shift);
   }
@@ -1009,7 +1016,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
   ops.nrm(col(0), D, beta + 0);
   for (int i = 1; i <= NOM; ++i) {
     ops.scale_inv(col(i - 1), D, beta + (i - 1));
-    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real, eft);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     if (i > 1) {
@@ -1091,7 +1098,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     for (int j = 0; j < NOK; ++j) hcb[j] = make_double2(cbeta[j + 1].real(), real ? 0.0 : cbeta[j + 1].imag());
     QS3G_CHECK_CUDA(cudaMemcpyAsync(cb, hcb.data(), NOK * sizeof(double2), cudaMemcpyHostToDevice, st));
     int i = NOK + 1;
-    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
+    HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real, eft);
     ++out.hv_count;
     ops.dot(col(i - 1), Q, D, alpha + i);
     ops.gemv_sub(V, ldv, NOK, cb, Q, D);
@@ -1100,7 +1107,7 @@ TrlanOut trlan_core(const Model& m, const Sector& s, T* V, int64_t ldv, T* Q, in
     ops.nrm(col(i), D, beta + i);
     for (i = NOK + 2; i <= NOM; ++i) {
       ops.scale_inv(col(i - 1), D, beta + (i - 1));
-      HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real);
+      HvOp<T>::apply(m, s, col(i - 1), Q, st, shift, real, eft);
       ++out.hv_count;
       ops.dot(col(i - 1), Q, D, alpha + i);
       ops.lanczos_w(col(i), Q, col(i - 1), col(i - 2), D, alpha + i, beta + (i - 1), false);

@@ -73,6 +73,8 @@ struct HvSeg {
   const uint32_t* tabc;
   const double* tcoef;
   const float* tcoef32;
+  const float2* tcoefS;     // split coefficients and phases (double-float table rows)
+  const float4* tphS;
   int tslots, tpacked;
 };
 
@@ -99,7 +101,8 @@ void hv32_seg(int NOD, const HvSeg* d_segs, const int* d_blk_seg, const int* d_b
 // true when the uniform form exists for NOD and uni
 bool seg_uniform_ok(int NOD, int uni);
 // uni = 4: every segment of the launch reads its connection table
-// (HvSeg::tab set, all packed or all wide)
+// (HvSeg::tab set); complex(8) vectors then take double-float arithmetic on
+// the FP32 pipe (the complex(8) phase of the lock-step batch)
 constexpr int kSegTable = 4;
 
 

@@ -120,12 +120,14 @@ struct HvTable {
   DevBuf<uint32_t> tab, tabc;
   DevBuf<double> coef;   // packed: coefficient per class
   DevBuf<float> coef32;
+  DevBuf<float2> coefS;  // coefficients (per class, or per bond * (NOD+1) + count) split hi + lo
+  DevBuf<float4> phS;    // chain phases split hi + lo (re, im)
   int slots = 0, deg = 0;
   bool packed = false;
   bool built() const { return slots > 0; }
   size_t bytes() const { return (tab.n + tabc.n) * sizeof(uint32_t); }
   void release() {
-    tab.release(); tabc.release(); coef.release(); coef32.release();
+    tab.release(); tabc.release(); coef.release(); coef32.release(); coefS.release(); phS.release();
     slots = deg = 0;
     packed = false;
   }
@@ -178,6 +180,11 @@ size_t hv_table_bytes(const Model& m, const Sector& s);
 bool build_hv_table(const Model& m, const Sector& s, HvTable& t, size_t keep, cudaStream_t st);
 
 void hv64(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+// The same from the cached connection table in double-float arithmetic on
+// the FP32 pipe (for the solvers' double-float modes); false, launching
+// nothing, when no table is cached.
+bool hv64_df(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);
+bool hv64r_df(const Model& m, const Sector& s, const double* x, double* y, cudaStream_t st, bool pad);
 // complex(4) H*v of H - shift (shift = 0 for the plain product)
 void hv32(const Model& m, const Sector& s, const float2* x, float2* y, cudaStream_t st, float shift = 0.f);
 void hv64_general(const Model& m, const Sector& s, const double2* x, double2* y, cudaStream_t st);

@@ -181,36 +181,37 @@ __global__ void k_anchor_to32(float2* __restrict__ v, const double2* __restrict_
 
 // Restart over B = [x, W[:, :nom]]: xn = B C[:, 0] in FP64 and
 // W[:, k-1] = B C[:, k] for k = 1..nout-1 in FP32 (in place: a block stages
-// its 32 rows of every input before writing).  C is (nom + 1) x nout,
-// column-major, split into float pairs in shared memory.
+// its kRestartRows rows of every input before writing).  C is (nom + 1) x
+// nout, column-major, already split into float pairs (re hi, re lo, im hi,
+// im lo) on the host, so no block spends FP64 instructions on it.
+constexpr int kRestartRows = 64;
+
 template <bool RE>
 __global__ void __launch_bounds__(256) k_anchor_restart(const double2* __restrict__ x, double2* __restrict__ xn,
                                                         float2* W, int64_t ldv, int nom, int nout,
-                                                        const double2* __restrict__ C, int64_t n) {
+                                                        const float4* __restrict__ C, int64_t n) {
   extern __shared__ float4 sma[];
+  constexpr int R = kRestartRows;
   const int nb = nom + 1;
   float4* cs = sma;                                                   // [nout][nb]
-  float4* xt = sma + (size_t)nb * nout;                               // [32]
-  float2* tile = reinterpret_cast<float2*>(xt + 32);                  // [nom][32]
-  const int64_t r0 = (int64_t)blockIdx.x * 32;
-  for (int k = threadIdx.x; k < nb * nout; k += blockDim.x) {
-    const float2 a = split(C[k].x), b = split(RE ? 0.0 : C[k].y);
-    cs[k] = make_float4(a.x, a.y, b.x, b.y);
-  }
-  for (int k = threadIdx.x; k < 32; k += blockDim.x) {
+  float4* xt = sma + (size_t)nb * nout;                               // [R]
+  float2* tile = reinterpret_cast<float2*>(xt + R);                   // [nom][R]
+  const int64_t r0 = (int64_t)blockIdx.x * R;
+  for (int k = threadIdx.x; k < nb * nout; k += blockDim.x) cs[k] = C[k];
+  for (int k = threadIdx.x; k < R; k += blockDim.x) {
     const int64_t i = r0 + k;
     xt[k] = (i < n) ? split2(x[i]) : make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  for (int k = threadIdx.x; k < nom * 32; k += blockDim.x) {
-    const int col = k / 32, r = k % 32;
+  for (int k = threadIdx.x; k < nom * R; k += blockDim.x) {
+    const int col = k / R, r = k % R;
     const int64_t i = r0 + r;
     tile[k] = (i < n) ? W[(int64_t)col * ldv + i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int r = threadIdx.x % R, g = threadIdx.x / R;
   const int64_t i = r0 + r;
   if (i >= n) return;
-  for (int oc = g; oc < nout; oc += 8) {
+  for (int oc = g; oc < nout; oc += 256 / R) {
     const float4* cc = cs + (size_t)oc * nb;
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
     {  // the FP64 anchor's row: (xr_hi + xr_lo, xi_hi + xi_lo) * c_0
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(256) k_anchor_restart(const double2* __restric
       }
     }
     for (int j = 0; j < nom; ++j) {
-      const float2 a = tile[j * 32 + r];
+      const float2 a = tile[j * R + r];
       const float4 c = cc[1 + j];
       df_add_prod(rh, rl, a.x, c.x);
       rl = fmaf(a.x, c.y, rl);
@@ -500,18 +501,29 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
       break;
     }
     // 5. new anchor and retained vectors in one pass over B
-    std::vector<double2> hC((size_t)NB * NOK);
+    // the coefficients split into float pairs here (hi = fl32(c), lo =
+    // fl32(c - hi), the device split's arithmetic), 16 bytes each
+    static_assert(sizeof(float4) == sizeof(double2), "split coefficients reuse the FP64 coefficient buffer");
+    std::vector<float4> hC((size_t)NB * NOK);
+    auto sp = [](double v) {
+      const float h = (float)v;
+      return std::make_pair(h, (float)(v - (double)h));
+    };
     for (int k = 0; k < NOK; ++k)
       for (int j = 0; j < NB; ++j) {
         const zd c = Cg[j + (size_t)k * NB];
-        hC[j + (size_t)k * NB] = make_double2(c.real(), real ? 0.0 : c.imag());
+        const auto a = sp(c.real()), b = sp(real ? 0.0 : c.imag());
+        hC[j + (size_t)k * NB] = make_float4(a.first, a.second, b.first, b.second);
       }
-    QS3G_CHECK_CUDA(cudaMemcpyAsync(sc.C.get(), hC.data(), hC.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
-    const size_t sm = (size_t)NB * NOK * sizeof(float4) + 32 * sizeof(float4) + (size_t)NOM * 32 * sizeof(float2);
+    float4* Cs = reinterpret_cast<float4*>(sc.C.get());
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(Cs, hC.data(), hC.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+    const size_t sm = (size_t)NB * NOK * sizeof(float4) + kRestartRows * sizeof(float4) +
+                      (size_t)NOM * kRestartRows * sizeof(float2);
     auto kern = real ? k_anchor_restart<true> : k_anchor_restart<false>;
     if (sm > 48 * 1024)
       QS3G_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    kern<<<(unsigned)((n + 31) / 32), 256, sm, st>>>(x, xn.get(), W.get(), ldv, NOM, NOK, sc.C.get(), n);
+    kern<<<(unsigned)((n + kRestartRows - 1) / kRestartRows), 256, sm, st>>>(x, xn.get(), W.get(), ldv, NOM, NOK,
+                                                                             Cs, n);
     check_launch("k_anchor_restart");
     QS3G_CHECK_CUDA(cudaMemcpyAsync(x, xn.get(), n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     o64.nrm(x, n, d_rn);

@@ -27,16 +27,23 @@ def random_chains(seed: int = 1, n: int = 256, L_range=(48, 128), nods=(3, 4, 5)
 
 
 def solve(problems, NOE=2, NOK=8, NOM=24, tol=1e-10, precision=1, maxitr=20000, nthreads=8, seed=1,
-          lockstep=False):
+          lockstep=False, hv_cache=False):
     """Build every sector, then solve all problems with qs3g_trlan_batch
     (concurrent streams) or, with lockstep=True, qs3g_trlan_lockstep (one
-    launch sequence for all problems).  Returns (records, build seconds,
-    solve seconds)."""
+    launch sequence for all problems).  hv_cache: cache each sector's
+    connection table first (qs3g_hv_cache; skipped where it does not fit).
+    Returns (records, build seconds, solve seconds)."""
     t0 = time.perf_counter()
     hs = []
     for p in problems:
         h = learned.chain_handle(p["L"], p["delta"], p["j2"])
         h.build_sector(p["nod"], (p["K"], 0, 0))
+        if hv_cache:
+            try:
+                h.hv_cache(True)
+            except capi.QS3GError as e:
+                if e.code != capi.ENOMEM:
+                    raise
         hs.append(h)
     t_build = time.perf_counter() - t0
     t0 = time.perf_counter()

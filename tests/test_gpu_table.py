@@ -81,6 +81,11 @@ def test_trlan_with_table(qs3g):
     r1 = h.trlan(2, 4, 12, maxitr=5000, tol=1e-10, precision=0, conv_mode=1, seed=3)
     a1 = h.trlan(1, 8, 24, maxitr=5000, tol=1e-10, precision=1, conv_mode=1, seed=3, real=True)
     assert np.array_equal(r0["ene"], r1["ene"]) and r0["iters"] == r1["iters"]
+    # the double-float modes read the table in double-float arithmetic
+    for prec, real in ((2, False), (2, True), (1, False)):
+        d = h.trlan(2, 4, 12, maxitr=5000, tol=1e-10, precision=prec, conv_mode=1, seed=3, real=real)
+        assert d["converged"] and d["resid"].max() <= 1e-10
+        np.testing.assert_allclose(d["ene"], r0["ene"], rtol=0, atol=1e-10 * abs(r0["ene"][0]))
     assert a1["converged"] and abs(a1["ene"][0] - a0["ene"][0]) <= 1e-10 * abs(a0["ene"][0])
     w = np.linalg.eigvalsh(O.Model(L, L, 1, 1, b, jxy, jz, kmax=nod + 2).build_sector(nod, (0, 0, 0)).dense())
     assert abs(a1["ene"][0] - w[0]) <= 1e-10 * abs(w[0])
