@@ -30,6 +30,8 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "eft.cuh"
@@ -179,17 +181,19 @@ __global__ void k_anchor_to32(float2* __restrict__ v, const double2* __restrict_
   }
 }
 
-// Restart over B = [x, W[:, :nom]]: xn = B C[:, 0] in FP64 and
-// W[:, k-1] = B C[:, k] for k = 1..nout-1 in FP32 (in place: a block stages
-// its kRestartRows rows of every input before writing).  C is (nom + 1) x
-// nout, column-major, already split into float pairs (re hi, re lo, im hi,
-// im lo) on the host, so no block spends FP64 instructions on it.
+// Restart over B = [x, W[:, :nom]]: xn = B C[:, 0] in FP64 (double-float
+// sums of split products) and W[:, k-1] = B C[:, k] for k = 1..nout-1 in
+// FP32 (fp32_out: plain FP32 sums of the hi parts; else double-float sums
+// rounded once), in place: a block stages its kRestartRows rows of every
+// input before writing.  C is (nom + 1) x nout, column-major, already split
+// into float pairs (re hi, re lo, im hi, im lo) on the host, so no block
+// spends FP64 instructions on it.
 constexpr int kRestartRows = 64;
 
 template <bool RE>
 __global__ void __launch_bounds__(256) k_anchor_restart(const double2* __restrict__ x, double2* __restrict__ xn,
                                                         float2* W, int64_t ldv, int nom, int nout,
-                                                        const float4* __restrict__ C, int64_t n) {
+                                                        const float4* __restrict__ C, int64_t n, int fp32_out) {
   extern __shared__ float4 sma[];
   constexpr int R = kRestartRows;
   const int nb = nom + 1;
@@ -213,6 +217,32 @@ __global__ void __launch_bounds__(256) k_anchor_restart(const double2* __restric
   if (i >= n) return;
   for (int oc = g; oc < nout; oc += 256 / R) {
     const float4* cc = cs + (size_t)oc * nb;
+    if (oc > 0 && fp32_out) {
+      // a retained vector is stored in FP32: plain FP32 sums (the anchor's
+      // row with its hi part and c's hi part), rounded once at the store
+      float re = 0.f, im = 0.f;
+      {
+        const float4 a = xt[r], c = cc[0];
+        re = fmaf(a.x, c.x, re);
+        im = fmaf(a.z, c.x, im);
+        if constexpr (!RE) {
+          re = fmaf(-a.z, c.z, re);
+          im = fmaf(a.x, c.z, im);
+        }
+      }
+      for (int j = 0; j < nom; ++j) {
+        const float2 a = tile[j * R + r];
+        const float4 c = cc[1 + j];
+        re = fmaf(a.x, c.x, re);
+        im = fmaf(a.y, c.x, im);
+        if constexpr (!RE) {
+          re = fmaf(-a.y, c.z, re);
+          im = fmaf(a.x, c.z, im);
+        }
+      }
+      W[(int64_t)(oc - 1) * ldv + i] = make_float2(re, im);
+      continue;
+    }
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
     {  // the FP64 anchor's row: (xr_hi + xr_lo, xi_hi + xi_lo) * c_0
       const float4 a = xt[r], c = cc[0];
@@ -314,6 +344,12 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   AnchorOut out;
   DevBuf<float2> W((size_t)ldv * (NOM + 1));
   DevBuf<double2> hx(n), hs(n), r(n), xn(n);
+  // The restart forms the retained vectors, stored in FP32, as plain FP32
+  // sums (the new anchor x' always in double-float).  At L = 1000 this took
+  // the same 13,582 H*v as double-float sums rounded once, in 50.2 s against
+  // 52.8 s; QS3G_ANCHOR_RESTART=df restores the double-float sums.
+  const char* rs_env = std::getenv("QS3G_ANCHOR_RESTART");
+  const bool restart_fp32 = !(rs_env && std::string(rs_env) == "df");
   Scratch sc;
   sc.ensure(NOM + 2);
   Ops<double2> o64{st, sc.part.get(), true, real};
@@ -523,7 +559,7 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
     if (sm > 48 * 1024)
       QS3G_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     kern<<<(unsigned)((n + kRestartRows - 1) / kRestartRows), 256, sm, st>>>(x, xn.get(), W.get(), ldv, NOM, NOK,
-                                                                             Cs, n);
+                                                                             Cs, n, restart_fp32 ? 1 : 0);
     check_launch("k_anchor_restart");
     QS3G_CHECK_CUDA(cudaMemcpyAsync(x, xn.get(), n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     o64.nrm(x, n, d_rn);
