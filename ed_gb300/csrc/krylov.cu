@@ -703,6 +703,12 @@ void Ops<T>::axpy(T* y, const T* x, int64_t n, const double2* a, double sgn) {
 template <class T>
 void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov) {
   if (ncols <= 0) return;
+  overlaps(V, ldv, ncols, w, n, ov);
+  gemv_sub(V, ldv, ncols, ov, w, n);
+}
+template <class T>
+void Ops<T>::overlaps(const T* V, int64_t ldv, int ncols, const T* w, int64_t n, double2* ov) {
+  if (ncols <= 0) return;
   int nb = kRedBlocks;
   if (kF32<T> || eft) {
     const int64_t tiles = (n + 255) / 256;
@@ -718,7 +724,6 @@ void Ops<T>::reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2
   check_launch("k_gemv_h_part");
   k_gemv_final<<<ncols, kRedThreads, 0, st>>>(part, nb, ncols, ov, real ? 1 : 0);
   check_launch("k_gemv_final");
-  gemv_sub(V, ldv, ncols, ov, w, n);
 }
 template <class T>
 void Ops<T>::gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n) {

@@ -39,6 +39,7 @@ struct Ops {
                  bool real_alpha);                                        // w = q - a v - b u
   void axpy(T* y, const T* x, int64_t n, const double2* a, double sgn);    // y += sgn*a*x
   void reorth(const T* V, int64_t ldv, int ncols, T* w, int64_t n, double2* ov);  // w -= V V^H w
+  void overlaps(const T* V, int64_t ldv, int ncols, const T* w, int64_t n, double2* ov);  // ov = V^H w
   void gemv_sub(const T* V, int64_t ldv, int ncols, const double2* coef, T* w, int64_t n);
   void restart(T* V, int64_t ldv, int nom, int nok, const double2* C, int64_t n);
   void random_start(T* x, int64_t n, uint64_t seed);
