@@ -50,6 +50,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def peaks_bf16():
+    """Measured dense BF16 tensor rate (burst), TFLOP/s; the fallback figure otherwise."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f).get("bf16_tflops", 1900.0))
+    return 1900.0
+
+
 def traffic_record():
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
@@ -431,6 +440,33 @@ def solve_arm(args):
                       "timed_out": st["timed_out"]}), flush=True)
 
 
+def mlp_inference_rate(net, h, D, delta, j2, reps=3):
+    """Tensor-core rate of the network's inference over the sector: D
+    representatives x NOD rotations, 2 (16*128 + 2*128*128 + 128) FLOP per
+    evaluation, CUDA-event time of the device-output prediction."""
+    import torch
+    from ed_gb300 import learned
+    dev = torch.device("cuda", torch.cuda.current_device())
+    vd = torch.empty(D, dtype=torch.complex128, device=dev)
+    c = learned.cond(delta, j2)
+    net.predict_device(h, *c, vd.data_ptr())
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        net.predict_device(h, *c, vd.data_ptr())
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    evals = D * NOD
+    flop = evals * 2 * (16 * 128 + 2 * 128 * 128 + 128)
+    peak = peaks_bf16()
+    tf = flop / (ms * 1e-3) / 1e12
+    del vd
+    return {"evaluations": evals, "ms": ms, "tflops": tf, "peak_bf16_tflops": peak,
+            "frac": tf / peak if peak else None}
+
+
 def solve_bench(args):
     """Ground state of the benchmark chain (L, N_down=4, k=0, Delta=0.5, J2=0.3,
     an unseen point of the network's training range) to ||H psi - E psi|| <= tol,
@@ -463,6 +499,7 @@ def solve_bench(args):
     t0 = time.perf_counter()
     v = learned.start_vector(net, h, delta, j2)
     out["network"]["predict_s"] = time.perf_counter() - t0
+    out["network"]["inference"] = mlp_inference_rate(net, h, D, delta, j2)
     if args.table:  # both arms read the cached connection table
         t0 = time.perf_counter()
         out["hv_table"] = {"bytes": h.hv_cache(True), "build_s": time.perf_counter() - t0}

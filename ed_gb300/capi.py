@@ -554,6 +554,11 @@ class Mlp:
         _check(load().qs3g_mlp_predict(self.h, handle.h, _ptr(cond), _ptr(v), _i(HOST)), handle.h)
         return v
 
+    def predict_device(self, handle, delta, j2, q0, v_ptr: int):
+        """The prediction into a device array of handle.D complex(8) values."""
+        cond = np.array([delta, j2, q0], np.float64)
+        _check(load().qs3g_mlp_predict(self.h, handle.h, _ptr(cond), C.c_void_p(v_ptr), _i(DEVICE)), handle.h)
+
 
 # ---------------------------------------------------------------- result files
 def _path(p):
