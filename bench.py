@@ -281,6 +281,16 @@ def run_gpu(args, rank, world, local_rank, dist):
         "clocks": clk.summary(),
     }
     line["hv_variants"] = hv_variants(h, x, D, stream, dev)
+    # the product the ground-state solve runs: real FP32 from the cached
+    # connection table, against HBM with the bytes it streams
+    tv = line["hv_variants"].get("table_real_f32")
+    if tv:
+        trt = traffic_record().get("hv_tab_real_f32", {})
+        line["roofline_table_real_f32"] = {
+            "bound": "hbm", "achieved": tv["stream_gbs"], "peak": peak, "unit": "GB/s",
+            "frac": tv["stream_gbs"] / peak, "peak_kind": peak_kind, "ms": tv["ms"],
+            "streamed_bytes": line["hv_variants"]["table"]["bytes"] + D * (2 * 4 + 16),
+            "traffic": trt.get("dram_bytes_per_launch"), "traffic_source": trt.get("source")}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"], line["parity"] = cpu_leg(args, h, x, y, D)
     h.close()
