@@ -46,7 +46,7 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kChunks = 304;       // row chunks of the overlap kernels (2 per SM) ...
-constexpr int kChunksNarrow = 1216;  // ... and for one or two columns (8 per SM, to fill the GPU)
+constexpr int kChunksNarrow = 1216;  // ... and for one or two columns (when the occupancy query fails)
 
 __device__ __forceinline__ float4 split2(double2 v) {
   const float2 r = dsplit(v.x), i = dsplit(v.y);
@@ -382,9 +382,20 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   QS3G_REQUIRE((size_t)(d_ov + (size_t)NS * (NOM + 1) - dsc.get()) <= dsc.n, QS3G_EINVAL, "scalar area");
   auto col = [&](int j) { return W.get() + (int64_t)j * ldv; };
   // conj(W[:, c0 .. c0+ncols)) . (v0, v1) into out[v * ncols + c]
+  // one or two columns: exactly one wave of resident blocks, so that no
+  // second, partly empty wave trails the first
+  int narrow = kChunksNarrow;
+  {
+    int dev = 0, sms = 0, per = 0;
+    QS3G_CHECK_CUDA(cudaGetDevice(&dev));
+    QS3G_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (real) QS3G_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_anchor_ovl<true>, kT, 0));
+    else QS3G_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_anchor_ovl<false>, kT, 0));
+    if (sms > 0 && per > 0) narrow = sms * per;
+  }
   auto ovl = [&](int c0, int ncols, const double2* v0, const double2* v1, double2* outp) {
     const int64_t tiles = (n + kT - 1) / kT;
-    const int nb = (int)std::min<int64_t>(ncols <= 2 ? kChunksNarrow : kChunks, tiles);
+    const int nb = (int)std::min<int64_t>(ncols <= 2 ? narrow : kChunks, tiles);
     const int64_t rows = (tiles + nb - 1) / nb * kT;
     const dim3 grid((unsigned)((ncols + 1) / 2), (unsigned)nb);
     if (real) k_anchor_ovl<true><<<grid, kT, 0, st>>>(col(c0), ldv, ncols, v0, v1, n, rows, part.get());
