@@ -11,10 +11,8 @@
 //   2. starts the extension from r orthogonalised against x and the retained
 //      vectors, and runs Lanczos steps on H - sigma (sigma = sum_b Jz_b/4, so
 //      the large common diagonal never enters an FP32 rounding) with FP32
-//      products and FP64-accurate (double-float) reductions; each product
-//      is orthogonalised against all of W in one classical Gram-Schmidt pass
-//      (its overlaps with the last two columns are alpha and beta) and
-//      against x;
+//      products and FP64-accurate (double-float) reductions and full
+//      reorthogonalisation against W and x;
 //   3. assembles the projected matrix G = B^H (H - sigma) B from the
 //      reorthogonalisation overlaps themselves (not from an assumed
 //      tridiagonal / arrowhead shape), with x's row computed exactly from
@@ -350,14 +348,6 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
   // sums (the new anchor x' always in double-float).  At L = 1000 this took
   // the same 13,582 H*v as double-float sums rounded once, in 50.2 s against
   // 52.8 s; QS3G_ANCHOR_RESTART=df restores the double-float sums.
-  // A step's product is orthogonalised against every basis column in one
-  // pass: alpha and beta are its overlaps with the last two columns, and the
-  // projected matrix takes all overlaps as they are.  The three-term update
-  // before it would only repeat that; at L = 1000 dropping it saved 5 %
-  // (47.8 s against 50.3 s, 13,514 against 13,582 H*v).
-  // QS3G_ANCHOR_STEP=three-term restores the update.
-  const char* st_env = std::getenv("QS3G_ANCHOR_STEP");
-  const bool gs_step = !(st_env && std::string(st_env) == "three-term");
   const char* rs_env = std::getenv("QS3G_ANCHOR_RESTART");
   const bool restart_fp32 = !(rs_env && std::string(rs_env) == "df");
   Scratch sc;
@@ -496,10 +486,8 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
         check_launch("k_anchor_axpy");
         o32.reorth(W.get(), ldv, i + 1, w, n, d_ov2);
       } else {
-        if (!gs_step) {
-          o32.dot(col(i), w, n, d_alpha + i);
-          o32.lanczos_w(w, w, col(i), col(i - 1), n, d_alpha + i, d_beta + (i - 1), false);
-        }
+        o32.dot(col(i), w, n, d_alpha + i);
+        o32.lanczos_w(w, w, col(i), col(i - 1), n, d_alpha + i, d_beta + (i - 1), false);
         o32.reorth(W.get(), ldv, i + 1, w, n, ov);
         ovl(i, 2, hs.get(), x, d_row + 4 * (size_t)i);
         k_anchor_axpy<<<grid_of(n), kT, 0, st>>>(w, x, n, d_row + 4 * (size_t)i + 3, real ? 1 : 0);
@@ -532,10 +520,8 @@ AnchorOut trlan_anchored(const Model& m, const Sector& s, const AnchorParams& p,
       if (i == ky) {
         for (int j = 0; j <= i; ++j) G[(1 + j) + (size_t)(1 + i) * NB] += cz(at(d_ov2)[j]);
       } else {
-        if (!gs_step) {
-          G[(1 + i) + (size_t)(1 + i) * NB] += at(d_alpha)[i].x;
-          G[i + (size_t)(1 + i) * NB] += at(d_beta)[i - 1].x;
-        }
+        G[(1 + i) + (size_t)(1 + i) * NB] += at(d_alpha)[i].x;
+        G[i + (size_t)(1 + i) * NB] += at(d_beta)[i - 1].x;
       }
       if (!(std::isfinite(at(d_beta)[i].x) && at(d_beta)[i].x > 0.0)) breakdown = true;
     }
