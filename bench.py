@@ -355,6 +355,13 @@ def hv_variants(h, x, D, stream, dev, reps=10):
         if name == "complex_f64":
             out["table_complex_f64"]["bit_identical_to_matrix_free"] = bool(torch.equal(yv, y_mf))
         del yv
+    # complex(8) from the table in double-float arithmetic (qs3g_hv_df)
+    ms, yv = timed(lambda a, b: h.hv_df_device(a, b), x)
+    B = D * 48 + nnz * 24
+    out["table_complex_f64_df"] = {
+        "ms": ms, "algorithmic_gbs": B / (ms * 1e-3) / 1e9, "stream_gbs": (nb + D * 48) / (ms * 1e-3) / 1e9,
+        "max_rel_dev_from_fp64": float((yv - y_mf).abs().max() / y_mf.abs().max())}
+    del yv
     h.hv_cache(False)
     return out
 

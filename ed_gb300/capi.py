@@ -37,7 +37,7 @@ EXPORTS = [
     "qs3g_mlp_loss_grad", "qs3g_mlp_train", "qs3g_mlp_align", "qs3g_mlp_predict", "qs3g_trlan_batch",
     "qs3g_trlan_lockstep", "qs3g_hv_schedule", "qs3g_hv_real", "qs3g_set_time_limit", "qs3g_trlan_stats",
     "qs3g_build_sector_i32", "qs3g_get_sector_i32", "qs3g_load_sector", "qs3g_load_sector_i32",
-    "qs3g_hv32_real", "qs3g_hv_cache",
+    "qs3g_hv32_real", "qs3g_hv_cache", "qs3g_hv_df",
 ]
 
 MLP_NPARAMS = 35329
@@ -291,6 +291,16 @@ class Handle:
         else:
             _check(rc, self.h)
         return dict(ene=ene, psi=psi, iters=int(iters.value), resid=resid, converged=(rc == OK))
+
+    def hv_df(self, x):
+        """H x from the cached connection table in double-float arithmetic."""
+        x = np.ascontiguousarray(x, np.complex128)
+        y = np.empty_like(x)
+        _check(load().qs3g_hv_df(self.h, _ptr(y), _ptr(x), _i(HOST)), self.h)
+        return y
+
+    def hv_df_device(self, x_ptr: int, y_ptr: int):
+        _check(load().qs3g_hv_df(self.h, C.c_void_p(y_ptr), C.c_void_p(x_ptr), _i(DEVICE)), self.h)
 
     def hv_cache(self, on=True):
         """Cache (or drop) the sector's connection table on the device; returns its bytes."""

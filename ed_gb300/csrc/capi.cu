@@ -361,6 +361,27 @@ int qs3g_hv(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where)
   });
 }
 
+int qs3g_hv_df(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where) {
+  return guarded(h, [&]() {
+    const Sector& s = need_sector(h);
+    QS3G_REQUIRE(v0 && v1 && where, QS3G_EINVAL, "null argument");
+    QS3G_REQUIRE(s.tab.built(), QS3G_ESTATE, "no connection table: call qs3g_hv_cache first");
+    if (*where == QS3G_DEVICE) {
+      hv64_df(h->model, s, reinterpret_cast<const double2*>(v1), reinterpret_cast<double2*>(v0), h->stream);
+      return QS3G_OK;
+    }
+    QS3G_REQUIRE(*where == QS3G_HOST, QS3G_EINVAL, "where must be QS3G_HOST or QS3G_DEVICE");
+    const size_t bytes = (size_t)s.D * sizeof(double2);
+    auto* x = static_cast<double2*>(staging(h, 0, bytes));
+    auto* y = static_cast<double2*>(staging(h, 1, bytes));
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(x, v1, bytes, cudaMemcpyHostToDevice, h->stream));
+    hv64_df(h->model, s, x, y, h->stream);
+    QS3G_CHECK_CUDA(cudaMemcpyAsync(v0, y, bytes, cudaMemcpyDeviceToHost, h->stream));
+    QS3G_CHECK_CUDA(cudaStreamSynchronize(h->stream));
+    return QS3G_OK;
+  });
+}
+
 int qs3g_hv_cache(qs3g_handle h, const int* on, int64_t* bytes) {
   return guarded(h, [&]() {
     QS3G_REQUIRE(h && h->sector, QS3G_ESTATE, "no sector: call qs3g_build_sector first");

@@ -79,6 +79,14 @@ module qs3g_iface
       integer(c_int) :: where
     end function
 
+    ! complex(8) H*v from the cached table in double-float arithmetic
+    integer(c_int) function qs3g_hv_df(h, v0, v1, where) bind(C, name="qs3g_hv_df")
+      import :: c_ptr, c_int, c_double_complex
+      type(c_ptr), value :: h
+      complex(c_double_complex) :: v0(*), v1(*)
+      integer(c_int) :: where
+    end function
+
     ! cache (on = 1) or drop (on = 0) the sector's connection table
     integer(c_int) function qs3g_hv_cache(h, on, bytes) bind(C, name="qs3g_hv_cache")
       import :: c_ptr, c_int, c_int64_t

@@ -174,6 +174,16 @@ int qs3g_hv_schedule(qs3g_handle h, const int* mode, int* chosen);
  * every hop at every product). */
 int qs3g_hv_cache(qs3g_handle h, const int* on, int64_t* bytes);
 
+/* The complex(8) product v0 = H v1 from the cached connection table in
+ * double-float arithmetic on the FP32 pipe (the arithmetic of qs3g_trlan's
+ * double-float modes): FP64 inputs split into float pairs with integer
+ * instructions, products and sums as unevaluated float pairs, about 2^-46
+ * relative instead of FP64's rounding.  GB300 executes FP64 at 1/64 of the
+ * FP32 rate and the FP64 product needs two FP64 FMAs per hop, so this form is
+ * bounded by HBM instead.  Not the reference's arithmetic: qs3g_hv is.
+ * QS3G_ESTATE without a cached table; where as for qs3g_hv. */
+int qs3g_hv_df(qs3g_handle h, qs3g_cplx* v0, const qs3g_cplx* v1, const int* where);
+
 /* The connection table of ham_to_vec_wave_vector: one entry per antiparallel
  * bond whose hop lands on a row of the sector (the `id > 0` branch of
  * source/ham2vec_v3.f90:61-65): 1-based row and column, the translation

@@ -116,3 +116,21 @@ def test_lockstep_row_forms_match_dense(qs3g, monkeypatch, form):
         w = np.linalg.eigvalsh(om.build_sector(p["nod"], (p["K"], 0, 0)).dense())
         assert abs(r["ene"][0] - w[0]) <= 1e-9 * max(1.0, abs(w[0])), (form, r["ene"], w[:3])
         assert max(r["resid"]) <= 1e-10
+
+
+@pytest.mark.parametrize("L,nod,K,J1,J2", CHAINS[:4])
+def test_double_float_table_product(qs3g, L, nod, K, J1, J2):
+    """qs3g_hv_df: the table product in double-float arithmetic stays within
+    a few 2^-46 of the FP64 product; it needs the cached table."""
+    from ed_gb300 import capi
+    h, D, _ = _handle(L, nod, K, J1, J2)
+    rng = np.random.default_rng(7 + K)
+    x = rng.standard_normal(D) + 1j * rng.standard_normal(D)
+    with pytest.raises(capi.QS3GError) as e:
+        h.hv_df(x)
+    assert e.value.code == capi.ESTATE
+    y = h.hv(x)
+    h.hv_cache(True)
+    yd = h.hv_df(x)
+    assert np.abs(yd - y).max() <= 1e-13 * np.abs(y).max()
+    h.close()
