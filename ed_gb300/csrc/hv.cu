@@ -580,13 +580,15 @@ __device__ __forceinline__ V tab_row(const TabArgs& t, const V* __restrict__ x, 
 // from pre-split tables, sums as unevaluated float pairs; one FP64 subtraction
 // (diagonal - shift) and the final joins per row.  GB300 runs FP64 at 1/64 of
 // the FP32 rate, and a k != 0 hop costs 6 FP64 operations in FP64.
-template <int NOD, bool PACKED, bool KZERO, class V = double2>
+template <int NOD, bool PACKED, bool KZERO, class V = double2, int SLOTS = 0>
 __device__ __forceinline__ V tab_row_df(const TabArgs& t, const V* __restrict__ x, int64_t i, double shift) {
   constexpr bool CPLX = sizeof(V) == sizeof(double2);
   int n[NOD];
   unpack<NOD>(__ldg(t.conf + i), t.bits, n);
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  for (int sl = 0; sl < t.slots; ++sl) {
+#pragma unroll
+  for (int sl = 0; sl < (SLOTS > 0 ? SLOTS : 64); ++sl) {
+    if (SLOTS == 0 && sl >= t.slots) break;
     const uint32_t e = __ldg(t.tab + (size_t)sl * t.D + i);
     int id, ell = 0;
     float2 c;
@@ -640,11 +642,11 @@ __device__ __forceinline__ V tab_row_df(const TabArgs& t, const V* __restrict__ 
   }
 }
 
-template <int NOD, bool PACKED, bool KZERO, class V>
+template <int NOD, bool PACKED, bool KZERO, class V, int SLOTS>
 __global__ void __launch_bounds__(kHvThreads) k_hv_tab_df(TabArgs t, const V* __restrict__ x, V* __restrict__ y,
                                                           int pad) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < t.D) y[i] = tab_row_df<NOD, PACKED, KZERO, V>(t, x, i, 0.0);
+  if (i < t.D) y[i] = tab_row_df<NOD, PACKED, KZERO, V, SLOTS>(t, x, i, 0.0);
   else if (i == t.D && pad) y[i] = V{};
 }
 
@@ -729,9 +731,18 @@ void launch_tab_df(const Model& m, const Sector& s, const V* x, V* y, int pad, c
   constexpr bool REAL = sizeof(V) == sizeof(double);
   dispatch_nod(s.NOD, [&](auto c) {
     constexpr int N = decltype(c)::value;
-    if (s.tab.packed) k_hv_tab_df<N, true, true, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
-    else if (s.kzero) k_hv_tab_df<N, false, true, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
-    else if constexpr (!REAL) k_hv_tab_df<N, false, false, V><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    constexpr int S4 = (N == 4 || N == 5) ? 4 * N : 0;  // four bonds per site, unrolled
+    const bool unr = S4 > 0 && a.slots == S4;
+    if (s.tab.packed) {
+      if (unr) k_hv_tab_df<N, true, true, V, S4><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+      else k_hv_tab_df<N, true, true, V, 0><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    } else if (s.kzero) {
+      if (unr) k_hv_tab_df<N, false, true, V, S4><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+      else k_hv_tab_df<N, false, true, V, 0><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    } else if constexpr (!REAL) {
+      if (unr) k_hv_tab_df<N, false, false, V, S4><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+      else k_hv_tab_df<N, false, false, V, 0><<<grid, kHvThreads, 0, st>>>(a, x, y, pad);
+    }
   });
   check_launch("k_hv_tab_df");
 }
@@ -793,7 +804,10 @@ __device__ __forceinline__ void seg_row(const HvSeg* __restrict__ segs, const in
       t.tcoef = g.tcoef; t.tcoef32 = g.tcoef32; t.chainph = g.chainph; t.chainph32 = g.chainph32;
       t.coefS = g.tcoefS; t.phS = g.tphS;
       if constexpr (F64) {
-        if (g.tpacked) ys[i] = tab_row_df<NOD, true, true>(t, xs, i, sh_);
+        constexpr int S4 = (NOD == 4 || NOD == 5) ? 4 * NOD : 0;
+        if (S4 > 0 && g.tslots == S4 && !g.tpacked && !g.kzero)  // the common k != 0 chain, unrolled
+          ys[i] = tab_row_df<NOD, false, false, V, S4>(t, xs, i, sh_);
+        else if (g.tpacked) ys[i] = tab_row_df<NOD, true, true>(t, xs, i, sh_);
         else if (g.kzero) ys[i] = tab_row_df<NOD, false, true>(t, xs, i, sh_);
         else ys[i] = tab_row_df<NOD, false, false>(t, xs, i, sh_);
       } else {
