@@ -226,24 +226,46 @@ __global__ void __launch_bounds__(kB) k_bgemv_sub(const BSeg* segs, const int* b
   int sg2;
   float nh = 0.f, nl = 0.f;
   if (brow(segs, bs, bf, r, sg2)) {
-    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    for (int k = 0; k < ncols; ++k) {
-      const float4 a = SplitLd<T>::ld(V[(int64_t)k * ldv + r]);
-      const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
-      const float4 ck = c[k];
-      const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
-      df_fma(rh, rl, cr, ar);
-      df_fma(rh, rl, fneg2(ci), ai);
-      df_fma(ih, il, cr, ai);
-      df_fma(ih, il, ci, ar);
+    T out;
+    if constexpr (sizeof(T) == sizeof(float2)) {
+      // complex(4) columns: FP32 FMAs with the coefficients' hi and lo parts
+      // summed apart (the single-problem subtraction's arithmetic); the
+      // result is stored in FP32 either way
+      const float2 wv = reinterpret_cast<const float2*>(w)[r];
+      float re = wv.x, im = wv.y, rlo = 0.f, ilo = 0.f;
+      for (int k = 0; k < ncols; ++k) {
+        const float2 a = reinterpret_cast<const float2*>(V)[(int64_t)k * ldv + r];
+        const float4 ck = c[k];
+        rlo = fmaf(-ck.y, a.x, rlo);
+        ilo = fmaf(-ck.y, a.y, ilo);
+        re = fmaf(-ck.x, a.x, re);
+        im = fmaf(-ck.x, a.y, im);
+        rlo = fmaf(ck.w, a.y, rlo);
+        ilo = fmaf(-ck.w, a.x, ilo);
+        re = fmaf(ck.z, a.y, re);
+        im = fmaf(-ck.z, a.x, im);
+      }
+      out = Store<T>::st(re, rlo, im, ilo);
+    } else {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int k = 0; k < ncols; ++k) {
+        const float4 a = SplitLd<T>::ld(V[(int64_t)k * ldv + r]);
+        const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+        const float4 ck = c[k];
+        const float2 cr = make_float2(ck.x, ck.y), ci = make_float2(ck.z, ck.w);
+        df_fma(rh, rl, cr, ar);
+        df_fma(rh, rl, fneg2(ci), ai);
+        df_fma(ih, il, cr, ai);
+        df_fma(ih, il, ci, ar);
+      }
+      const float4 wv = SplitLd<T>::ld(w[r]);
+      float wrh = wv.x, wrl = wv.y, wih = wv.z, wil = wv.w;
+      df_add(wrh, wrl, -rh);
+      wrl = __fsub_rn(wrl, rl);
+      df_add(wih, wil, -ih);
+      wil = __fsub_rn(wil, il);
+      out = Store<T>::st(wrh, wrl, wih, wil);
     }
-    const float4 wv = SplitLd<T>::ld(w[r]);
-    float wrh = wv.x, wrl = wv.y, wih = wv.z, wil = wv.w;
-    df_add(wrh, wrl, -rh);
-    wrl = __fsub_rn(wrl, rl);
-    df_add(wih, wil, -ih);
-    wil = __fsub_rn(wil, il);
-    const T out = Store<T>::st(wrh, wrl, wih, wil);
     w[r] = out;
     if (npart) {
       const float4 a = SplitLd<T>::ld(out);
@@ -288,15 +310,28 @@ __global__ void __launch_bounds__(kB) k_brestart(const BSeg* segs, const int* bs
     if (li < g.D) {
       for (int oc = grp; oc < nok; oc += kB / 32) {
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-        for (int j = 0; j < nom; ++j) {
-          const float4 a = tile[j * 32 + rr];
-          const float4 c = cs[(size_t)oc * nom + j];
-          const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
-          const float2 cr = make_float2(c.x, c.y), ci = make_float2(c.z, c.w);
-          df_fma(rh, rl, ar, cr);
-          df_fma(rh, rl, fneg2(ai), ci);
-          df_fma(ih, il, ar, ci);
-          df_fma(ih, il, ai, cr);
+        if constexpr (sizeof(T) == sizeof(float2)) {
+          // complex(4) outputs: plain FP32 sums of the hi parts (they are
+          // stored in FP32)
+          for (int j = 0; j < nom; ++j) {
+            const float4 a = tile[j * 32 + rr];
+            const float4 c = cs[(size_t)oc * nom + j];
+            rh = fmaf(a.x, c.x, rh);
+            rh = fmaf(-a.z, c.z, rh);
+            ih = fmaf(a.x, c.z, ih);
+            ih = fmaf(a.z, c.x, ih);
+          }
+        } else {
+          for (int j = 0; j < nom; ++j) {
+            const float4 a = tile[j * 32 + rr];
+            const float4 c = cs[(size_t)oc * nom + j];
+            const float2 ar = make_float2(a.x, a.y), ai = make_float2(a.z, a.w);
+            const float2 cr = make_float2(c.x, c.y), ci = make_float2(c.z, c.w);
+            df_fma(rh, rl, ar, cr);
+            df_fma(rh, rl, fneg2(ai), ci);
+            df_fma(ih, il, ar, ci);
+            df_fma(ih, il, ai, cr);
+          }
         }
         V[(int64_t)oc * ldv + g.row0 + li] = Store<T>::st(rh, rl, ih, il);
       }
