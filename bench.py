@@ -672,7 +672,7 @@ def dsf_bench():
             "spectral_weight_finite": bool(np.isfinite(S[1:]).all())}
 
 
-def main():
+def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -681,8 +681,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-solve", dest="solve", action="store_false",
-                    help="skip the ground-state solves (learned start + complex(4) storage vs plain FP64 "
-                         "random start; about 20 minutes, on by default)")
+                    help="skip the ground-state solves (learned start + anchored FP32 solver vs plain FP64 "
+                         "random start; about 16 minutes, on by default)")
     ap.add_argument("--solve-all", action="store_true",
                     help="with the solves, also the complex-vector, random-start and real FP64 arms")
     ap.add_argument("--dsf", action="store_true", help="add the all-q DSF batch (L=200, 200 q, 150 levels)")
@@ -705,7 +705,11 @@ def main():
                     help="wall seconds after which the plain FP64 solve stops (reported as a lower bound)")
     ap.add_argument("--L", type=int, default=1000,
                     help="chain length (1000 is the benchmark; smaller sizes are for profiling)")
-    args = ap.parse_args()
+    return ap.parse_args()
+
+
+def main():
+    args = parse_args()
     global L_SITES, WORKLOAD
     if args.L != L_SITES:
         L_SITES = args.L

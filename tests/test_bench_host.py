@@ -49,3 +49,33 @@ def test_single_process_defaults():
     r, w, lr, dist = bench.dist_setup()
     assert (r, w, dist) == (0, 1, None)
     assert bench.max_over_ranks(3.0, None) == 3.0
+
+
+def test_peaks_and_traffic_records():
+    """The roofline denominators and the ncu traffic records the bench line
+    cites: measured peaks when present, and a traffic entry for each kernel
+    it reports a roofline for."""
+    import bench
+    hbm, kind = bench.peaks()
+    assert hbm > 1000.0 and kind in ("measured", "fallback")
+    assert bench.peaks_bf16() > 100.0
+    tr = bench.traffic_record()
+    for k in ("hv_chain64", "hv_tab_real_f32"):
+        assert tr[k]["dram_bytes_per_launch"] > 1e9 and "ncu" in tr[k]["source"]
+
+
+def test_arguments_of_the_optional_legs():
+    """--batch, --cfg5, --dsf and --no-table parse; the default runs the
+    ground-state solve with the connection table."""
+    import sys
+    import bench
+    old = sys.argv
+    try:
+        sys.argv = ["bench.py"]
+        a = bench.parse_args()
+        assert a.solve and a.table and not a.batch and not a.cfg5 and a.batch_n == 256
+        sys.argv = ["bench.py", "--batch", "--batch-n", "64", "--no-table", "--cfg5", "--dsf", "--no-solve"]
+        a = bench.parse_args()
+        assert a.batch and a.batch_n == 64 and not a.table and a.cfg5 and a.dsf and not a.solve
+    finally:
+        sys.argv = old
