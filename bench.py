@@ -460,7 +460,9 @@ def solve_arm(args):
 def mlp_inference_rate(net, h, D, delta, j2, reps=3):
     """Tensor-core rate of the network's inference over the sector: D
     representatives x NOD rotations, 2 (16*128 + 2*128*128 + 128) FLOP per
-    evaluation, CUDA-event time of the device-output prediction."""
+    evaluation over the time of a device-output prediction call.  The call
+    returns when its work is done, so the events bracket it whole, including
+    its host-side staging: a lower bound on the kernels' rate."""
     import torch
     from ed_gb300 import learned
     dev = torch.device("cuda", torch.cuda.current_device())
